@@ -1,0 +1,88 @@
+"""ctypes binding of libcritic2_gb300.so (the C ABI in include/critic2_gb300.h).
+
+Loading fails loudly when the library has not been built: there is no
+CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcritic2_gb300.so")
+
+C2G_OK = 0
+PREC = {"fp64": 0, "tf32x3": 1, "bf16x3": 2}
+ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported"}
+
+# every symbol include/critic2_gb300.h declares
+EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx",
+           "c2g_wfn_destroy", "c2g_wfn_info", "c2g_rho2", "c2g_grd", "c2g_nciplot",
+           "c2g_nciplot_dev", "c2g_newton", "c2g_pair_seeds", "c2g_autocritic")
+
+
+class C2GError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"critic2_gb300 error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class NciStats(C.Structure):
+    _fields_ = [("npoints", C.c_long), ("nrecheck", C.c_long), ("ms_kernel", C.c_double),
+                ("ms_recheck", C.c_double)]
+
+
+class CpReport(C.Structure):
+    _fields_ = [("ncp", C.c_int), ("count", C.c_int * 4), ("poincare_hopf", C.c_int),
+                ("nseed", C.c_int), ("nconverged", C.c_int), ("ms_total", C.c_double)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+_lib = None
+
+
+def lib():
+    """Loads the shared library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with critic2_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    L.c2g_abi_version.restype = C.c_int
+    L.c2g_last_error.argtypes = [C.c_char_p, C.c_int]
+    L.c2g_wfn_create.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp,
+                                 C.c_int, C.c_int, C.POINTER(_vp)]
+    L.c2g_wfn_read_wfx.argtypes = [C.c_char_p, C.POINTER(_vp)]
+    L.c2g_wfn_destroy.argtypes = [_vp]
+    L.c2g_wfn_info.argtypes = [_vp] + [C.POINTER(C.c_int)] * 5
+    L.c2g_rho2.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int] + [_vp] * 6
+    L.c2g_grd.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int] + [_vp] * 8
+    L.c2g_nciplot.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, C.POINTER(NciStats)]
+    L.c2g_nciplot_dev.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, _vp, C.POINTER(NciStats)]
+    L.c2g_newton.argtypes = [_vp, C.c_int, _vp, C.c_double, C.c_int, C.c_int, _vp]
+    L.c2g_pair_seeds.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(C.c_int)]
+    L.c2g_autocritic.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int, _vp, _vp, _vp,
+                                 C.POINTER(CpReport)]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    lib().c2g_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int):
+    if rc != C2G_OK:
+        raise C2GError(rc, last_error())
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(_vp)

@@ -1,0 +1,479 @@
+// C-ABI entry points of critic2_gb300 (declared in include/critic2_gb300.h).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "c2g_internal.h"
+#include "k_tc.h"
+
+namespace c2g {
+
+namespace {
+thread_local std::string g_last_error;
+
+// Keeps the caller's current device and restores it on exit.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    C2G_CUDA(cudaGetDevice(&prev));
+    if (prev != dev) C2G_CUDA(cudaSetDevice(dev));
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+template <class T>
+T *dev_alloc(Handle &h, size_t n) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) fail(C2G_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  h.allocations.push_back(p);
+  return static_cast<T *>(p);
+}
+
+template <class T>
+T *upload(Handle &h, const std::vector<T> &v) {
+  T *d = dev_alloc<T>(h, v.size());
+  if (!v.empty()) C2G_CUDA(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return d;
+}
+
+// Scratch device buffer owned by one call.
+struct DevBuf {
+  void *p = nullptr;
+  explicit DevBuf(size_t bytes) {
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+    if (e != cudaSuccess) fail(C2G_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+void require(bool ok, const char *msg) {
+  if (!ok) fail(C2G_ERR_ARG, msg);
+}
+
+void build_device(Handle &h) {
+  HostWfn &w = h.host;
+  C2G_CUDA(cudaGetDevice(&h.device));
+  DevWfn &d = h.dev;
+  d.natom = w.natom;
+  d.npri = w.npri;
+  d.nmo = w.nmo;
+  d.nmo_pad = (w.nmo + 63) / 64 * 64;
+  std::vector<double4> atoms(w.natom);
+  for (int a = 0; a < w.natom; a++)
+    atoms[a] = make_double4(w.xyz[3 * a], w.xyz[3 * a + 1], w.xyz[3 * a + 2],
+                            w.spcutoff[a] * w.spcutoff[a]);
+  d.atoms = upload(h, atoms);
+  d.atom_z = upload(h, w.z);
+  std::vector<PrimF64> prim(w.npri);
+  std::vector<double> cmo((size_t)w.npri * d.nmo_pad, 0.0);
+  for (int k = 0; k < w.npri; k++) {
+    const int ip = w.icord[k];
+    const int *l = kLi[w.itype[ip] - 1];
+    prim[k] = PrimF64{w.e[ip], w.dran[ip], l[0] | (l[1] << 4) | (l[2] << 8), w.icenter[ip], 0, 0};
+    std::copy(w.cmo.begin() + (size_t)ip * w.nmo, w.cmo.begin() + (size_t)(ip + 1) * w.nmo,
+              cmo.begin() + (size_t)k * d.nmo_pad);
+  }
+  d.prim = upload(h, prim);
+  d.cmo = upload(h, cmo);
+  std::vector<double> occ(d.nmo_pad, 0.0), wup(d.nmo_pad, 0.0), wdn(d.nmo_pad, 0.0);
+  for (int m = 0; m < w.nmo; m++) {
+    occ[m] = w.occ[m];
+    const bool alpha = m < w.nalpha;
+    if (w.wfntyp == C2G_WFN_UHF) (alpha ? wup : wdn)[m] = w.occ[m];
+    else if (w.wfntyp == C2G_WFN_ROHF) {
+      wup[m] = w.occ[m];
+      if (alpha) wdn[m] = w.occ[m];
+    }
+  }
+  d.occ = upload(h, occ);
+  d.spin = (w.wfntyp == C2G_WFN_UHF || w.wfntyp == C2G_WFN_ROHF);
+  d.wup = d.spin ? upload(h, wup) : nullptr;
+  d.wdn = d.spin ? upload(h, wdn) : nullptr;
+  for (int j = 0; j < 3; j++) d.cell_lo[j] = w.cell_lo[j], d.cell_aa[j] = w.cell_aa[j];
+}
+
+Handle *check_handle(c2g_wfn *hp) {
+  require(hp != nullptr, "null handle");
+  return reinterpret_cast<Handle *>(hp);
+}
+
+int check_prec(int prec) {
+  require(prec == C2G_PREC_FP64 || prec == C2G_PREC_TF32X3 || prec == C2G_PREC_BF16X3,
+          "unknown precision mode");
+  return prec;
+}
+
+// Evaluates the FP64 record (kRecFull when full) at n host points.
+std::vector<double> eval_records_fp64(Handle &h, int n, const double *xyz, int nder, bool full) {
+  const int nr = full ? kRecFull : kRecNci;
+  DevBuf dx(sizeof(double) * 3 * (size_t)n), dr(sizeof(double) * nr * (size_t)n);
+  C2G_CUDA(cudaMemcpy(dx.p, xyz, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice));
+  launch_fp64_points(h.dev, n, dx.as<double>(), nder, full, dr.as<double>(), 0);
+  std::vector<double> rec((size_t)nr * n);
+  C2G_CUDA(cudaMemcpy(rec.data(), dr.p, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost));
+  return rec;
+}
+
+// Records at n host points in the requested precision; the split modes give
+// the kRecNci quantities only.
+std::vector<double> eval_records(Handle &h, int n, const double *xyz, int nder, int prec, bool full) {
+  if (prec == C2G_PREC_FP64) return eval_records_fp64(h, n, xyz, nder, full);
+  const int nr = kRecNci;
+  DevBuf dx(sizeof(double) * 3 * (size_t)n), dr(sizeof(double) * nr * (size_t)n);
+  C2G_CUDA(cudaMemcpy(dx.p, xyz, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice));
+  tc_points(h, prec, n, dx.as<double>(), dr.as<double>(), 0);
+  std::vector<double> rec((size_t)nr * n);
+  C2G_CUDA(cudaMemcpy(rec.data(), dr.p, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost));
+  if (full) {
+    std::vector<double> out((size_t)kRecFull * n, 0.0);
+    for (int i = 0; i < n; i++)
+      std::copy(rec.begin() + (size_t)i * nr, rec.begin() + (size_t)(i + 1) * nr,
+                out.begin() + (size_t)i * kRecFull);
+    return out;
+  }
+  return rec;
+}
+
+}  // namespace
+
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+const std::string &last_error() { return g_last_error; }
+
+void fail(int code, const std::string &msg) { throw Failure(code, msg); }
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) fail(C2G_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Symmetric 3x3 eigenvalues (column-major input), ascending; cyclic Jacobi.
+void eigsym3(const double m[9], double ev[3]) {
+  double a[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) a[i][j] = 0.5 * (m[3 * j + i] + m[3 * i + j]);
+  for (int sweep = 0; sweep < 60; sweep++) {
+    const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    const double dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off == 0.0 || off < 1e-34 * dia) break;
+    for (int p = 0; p < 2; p++)
+      for (int q = p + 1; q < 3; q++) {
+        if (a[p][q] == 0.0) continue;
+        const double th = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; k++) {
+          const double kp = a[k][p], kq = a[k][q];
+          a[k][p] = c * kp - s * kq;
+          a[k][q] = s * kp + c * kq;
+        }
+        for (int k = 0; k < 3; k++) {
+          const double pk = a[p][k], qk = a[q][k];
+          a[p][k] = c * pk - s * qk;
+          a[q][k] = s * pk + c * qk;
+        }
+      }
+  }
+  double e[3] = {a[0][0], a[1][1], a[2][2]};
+  std::sort(e, e + 3);
+  ev[0] = e[0], ev[1] = e[1], ev[2] = e[2];
+}
+
+// The rho2 output assembly (src/wfn_private@proc.F90:2636-2703) from a
+// kRecFull record, for one point.
+static void assemble_rho2(const HostWfn &w, const double *r, int nder, double *rho, double *grad,
+                          double *hess, double *gkin, double *stress, double *vir) {
+  const bool spin = (w.wfntyp == C2G_WFN_UHF || w.wfntyp == C2G_WFN_ROHF);
+  double rh[3], g[3][3], hh[3][6], gk[3];
+  rh[0] = r[0];
+  for (int j = 0; j < 3; j++) g[0][j] = r[1 + j];
+  for (int j = 0; j < 6; j++) hh[0][j] = r[4 + j];
+  gk[0] = r[10];
+  if (spin) {
+    for (int s = 0; s < 2; s++) {
+      const double *b = r + 17 + 11 * s;
+      rh[1 + s] = b[0];
+      for (int j = 0; j < 3; j++) g[1 + s][j] = b[1 + j];
+      gk[1 + s] = b[4];
+      for (int j = 0; j < 6; j++) hh[1 + s][j] = b[5 + j];
+    }
+  } else {
+    rh[1] = rh[2] = 0.5 * rh[0];
+    for (int j = 0; j < 3; j++) g[1][j] = g[2][j] = 0.5 * g[0][j];
+    for (int j = 0; j < 6; j++) hh[1][j] = hh[2][j] = 0.5 * hh[0][j];
+    gk[1] = gk[2] = gk[0] / 2.0;
+  }
+  if (rho)
+    for (int s = 0; s < 3; s++) rho[s] = rh[s];
+  if (grad && nder > 0)
+    for (int s = 0; s < 3; s++)
+      for (int j = 0; j < 3; j++) grad[3 * s + j] = g[s][j];
+  if (gkin && nder > 0)
+    for (int s = 0; s < 3; s++) gkin[s] = 0.5 * gk[s];
+  if (hess && nder > 1)
+    for (int s = 0; s < 3; s++) {
+      double *H = hess + 9 * s;
+      H[0] = hh[s][0], H[4] = hh[s][1], H[8] = hh[s][2];
+      H[1] = H[3] = hh[s][3], H[2] = H[6] = hh[s][4], H[5] = H[7] = hh[s][5];
+    }
+  if (nder > 1 && (stress || vir)) {
+    // r[11..16] = xx, xy, xz, yy, yz, zz, halved at the end
+    const double sxx = 0.5 * r[11], sxy = 0.5 * r[12], sxz = 0.5 * r[13];
+    const double syy = 0.5 * r[14], syz = 0.5 * r[15], szz = 0.5 * r[16];
+    if (stress) {
+      stress[0] = sxx, stress[1] = sxy, stress[2] = sxz;
+      stress[3] = sxy, stress[4] = syy, stress[5] = syz;
+      stress[6] = sxz, stress[7] = syz, stress[8] = szz;
+    }
+    if (vir) *vir = sxx + syy + szz;
+  }
+}
+
+}  // namespace c2g
+
+using namespace c2g;
+
+extern "C" {
+
+int c2g_abi_version(void) { return C2G_ABI_VERSION; }
+
+int c2g_last_error(char *buf, int len) {
+  const int n = (int)g_last_error.size();
+  if (buf && len > 0) {
+    const int m = std::min(n, len - 1);
+    std::memcpy(buf, g_last_error.data(), m);
+    buf[m] = 0;
+  }
+  return n;
+}
+
+int c2g_wfn_create(int natom, const double *atom_xyz, const int *atom_z, int npri, int nmo,
+                   const int *icenter, const int *itype, const double *e, const double *occ,
+                   const double *cmo, int wfntyp, int nalpha, c2g_wfn **out) {
+  return guarded([&] {
+    require(out != nullptr, "null output handle pointer");
+    *out = nullptr;
+    require(natom > 0 && npri > 0 && nmo > 0, "natom, npri and nmo must be positive");
+    require(atom_xyz && atom_z && icenter && itype && e && occ && cmo, "null input array");
+    require(wfntyp >= 0 && wfntyp <= 3, "unknown wavefunction type");
+    auto h = std::make_unique<Handle>();
+    HostWfn &w = h->host;
+    w.natom = natom, w.npri = npri, w.nmo = nmo, w.wfntyp = wfntyp, w.nalpha = nalpha;
+    w.xyz.assign(atom_xyz, atom_xyz + 3 * (size_t)natom);
+    w.z.assign(atom_z, atom_z + natom);
+    w.icenter.resize(npri);
+    w.itype.assign(itype, itype + npri);
+    w.e.assign(e, e + npri);
+    w.occ.assign(occ, occ + nmo);
+    w.cmo.assign(cmo, cmo + (size_t)npri * nmo);
+    for (int i = 0; i < npri; i++) {
+      require(icenter[i] >= 1 && icenter[i] <= natom, "icenter out of range");
+      require(itype[i] >= 1 && itype[i] <= 56, "itype out of range (1..56)");
+      require(e[i] > 0.0, "exponents must be positive");
+      w.icenter[i] = icenter[i] - 1;
+    }
+    prune_primitives(w);
+    complete_struct(w);
+    molecular_cell(w);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      fail(C2G_ERR_CUDA, "no CUDA device available");
+    }
+    try {
+      build_device(*h);
+      h->tc = tc_create(*h);
+    } catch (...) {
+      for (void *p : h->allocations) cudaFree(p);
+      if (h->tc) tc_destroy(h->tc);
+      throw;
+    }
+    *out = reinterpret_cast<c2g_wfn *>(h.release());
+  });
+}
+
+int c2g_wfn_read_wfx(const char *path, c2g_wfn **out) {
+  return guarded([&] {
+    require(path && out, "null argument");
+    HostWfn w;
+    std::string err;
+    if (!read_wfx(path, w, err)) fail(C2G_ERR_IO, err);
+    // read_wfx already pruned; create re-runs prune (idempotent) on the
+    // original-order arrays.
+    std::vector<int> icenter1(w.npri);
+    for (int i = 0; i < w.npri; i++) icenter1[i] = w.icenter[i] + 1;
+    int rc = c2g_wfn_create(w.natom, w.xyz.data(), w.z.data(), w.npri, w.nmo, icenter1.data(),
+                            w.itype.data(), w.e.data(), w.occ.data(), w.cmo.data(), w.wfntyp,
+                            w.nalpha, out);
+    if (rc != C2G_OK) fail(rc, g_last_error);
+  });
+}
+
+int c2g_wfn_destroy(c2g_wfn *hp) {
+  return guarded([&] {
+    if (!hp) return;
+    Handle *h = reinterpret_cast<Handle *>(hp);
+    {
+      DeviceGuard g(h->device);
+      if (h->tc) tc_destroy(h->tc);
+      for (void *p : h->allocations) cudaFree(p);
+    }
+    delete h;
+  });
+}
+
+int c2g_wfn_info(const c2g_wfn *hp, int *natom, int *npri, int *nmo, int *wfntyp, int *nalpha) {
+  return guarded([&] {
+    require(hp != nullptr, "null handle");
+    const Handle *h = reinterpret_cast<const Handle *>(hp);
+    if (natom) *natom = h->host.natom;
+    if (npri) *npri = h->host.npri;
+    if (nmo) *nmo = h->host.nmo;
+    if (wfntyp) *wfntyp = h->host.wfntyp;
+    if (nalpha) *nalpha = h->host.nalpha;
+  });
+}
+
+int c2g_rho2(c2g_wfn *hp, int n, const double *xyz, int nder, int prec, double *rho, double *grad,
+             double *hess, double *gkin, double *stress, double *vir) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(n >= 0, "negative point count");
+    require(nder >= 0 && nder <= 2, "nder must be 0, 1 or 2");
+    check_prec(prec);
+    if (n == 0) return;
+    require(xyz != nullptr, "null xyz");
+    DeviceGuard g(h->device);
+    const bool full = (prec == C2G_PREC_FP64);
+    std::vector<double> rec = eval_records(*h, n, xyz, nder, prec, true);
+    (void)full;
+    for (int i = 0; i < n; i++)
+      assemble_rho2(h->host, rec.data() + (size_t)i * kRecFull, nder, rho ? rho + 3 * i : nullptr,
+                    grad ? grad + 9 * i : nullptr, hess ? hess + 27 * i : nullptr,
+                    gkin ? gkin + 3 * i : nullptr, stress ? stress + 9 * i : nullptr,
+                    vir ? vir + i : nullptr);
+  });
+}
+
+int c2g_grd(c2g_wfn *hp, int n, const double *xyz, int nder, int prec, double *f, double *gf,
+            double *gfmod, double *hf, double *hfeval, int *r, int *s, int *isnuc) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(n >= 0, "negative point count");
+    require(nder >= 0 && nder <= 2, "nder must be 0, 1 or 2");
+    check_prec(prec);
+    if (n == 0) return;
+    require(xyz != nullptr, "null xyz");
+    DeviceGuard g(h->device);
+    std::vector<double> rec = eval_records(*h, n, xyz, nder, prec, false);
+    const HostWfn &w = h->host;
+    for (int i = 0; i < n; i++) {
+      const double *q = rec.data() + (size_t)i * kRecNci;
+      // wrapped position (as the kernel evaluated it) for the nucleus test
+      double x[3];
+      for (int j = 0; j < 3; j++) {
+        double fr = (xyz[3 * i + j] - w.cell_lo[j]) / w.cell_aa[j];
+        if (fr < -1e-4 || fr > 1.0 + 1e-4) fr -= std::floor(fr);
+        x[j] = w.cell_lo[j] + fr * w.cell_aa[j];
+      }
+      bool nuc = false;
+      for (int a = 0; a < w.natom && !nuc; a++) {
+        const double dx = x[0] - w.xyz[3 * a], dy = x[1] - w.xyz[3 * a + 1], dz = x[2] - w.xyz[3 * a + 2];
+        nuc = std::sqrt(dx * dx + dy * dy + dz * dz) <= 1e-5;
+      }
+      if (f) f[i] = q[0];
+      if (isnuc) isnuc[i] = nuc;
+      double gg[3] = {q[1], q[2], q[3]};
+      if (nuc) gg[0] = gg[1] = gg[2] = 0.0;
+      if (gf && nder > 0)
+        for (int j = 0; j < 3; j++) gf[3 * i + j] = gg[j];
+      if (gfmod) gfmod[i] = nder > 0 ? std::sqrt(gg[0] * gg[0] + gg[1] * gg[1] + gg[2] * gg[2]) : 0.0;
+      if (nder > 1) {
+        double H[9] = {q[4], q[7], q[8], q[7], q[5], q[9], q[8], q[9], q[6]};
+        if (hf) std::copy(H, H + 9, hf + 9 * i);
+        double ev[3];
+        eigsym3(H, ev);
+        if (hfeval) std::copy(ev, ev + 3, hfeval + 3 * i);
+        int np = 0, nm = 0;
+        for (double v : ev) np += v > 1e-8, nm += v < -1e-8;
+        if (r) r[i] = np + nm;
+        if (s) s[i] = np - nm;
+      }
+    }
+  });
+}
+
+int c2g_nciplot_dev(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec,
+                    double *d_crho, double *d_cgrad, void *stream, c2g_nci_stats *stats) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(x0 && xmat && nstep && d_crho && d_cgrad, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    require((long)nstep[0] * nstep[1] * nstep[2] < (1L << 31), "grid too large (2^31 points)");
+    check_prec(prec);
+    DeviceGuard g(h->device);
+    GridSpec gs;
+    for (int j = 0; j < 3; j++) gs.x0[j] = x0[j], gs.nstep[j] = nstep[j];
+    for (int j = 0; j < 9; j++) gs.xmat[j] = xmat[j];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    if (stats) {
+      C2G_CUDA(cudaEventCreate(&e0));
+      C2G_CUDA(cudaEventCreate(&e1));
+      C2G_CUDA(cudaEventCreate(&e2));
+      C2G_CUDA(cudaEventRecord(e0, st));
+    }
+    long nrecheck = 0;
+    if (prec == C2G_PREC_FP64) {
+      launch_fp64_nci_grid(h->dev, gs, d_crho, d_cgrad, st);
+      if (stats) C2G_CUDA(cudaEventRecord(e1, st));
+    } else {
+      nrecheck = tc_nci_grid(*h, prec, gs, d_crho, d_cgrad, st, stats ? e1 : nullptr);
+    }
+    if (stats) {
+      C2G_CUDA(cudaEventRecord(e2, st));
+      C2G_CUDA(cudaEventSynchronize(e2));
+      float a = 0.f, b = 0.f;
+      C2G_CUDA(cudaEventElapsedTime(&a, e0, e1));
+      C2G_CUDA(cudaEventElapsedTime(&b, e1, e2));
+      stats->npoints = (long)nstep[0] * nstep[1] * nstep[2];
+      stats->nrecheck = nrecheck;
+      stats->ms_kernel = a;
+      stats->ms_recheck = b;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cudaEventDestroy(e2);
+    }
+  });
+}
+
+int c2g_nciplot(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec,
+                double *crho, double *cgrad, c2g_nci_stats *stats) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(x0 && xmat && nstep && crho && cgrad, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    DeviceGuard g(h->device);
+    const size_t np = (size_t)nstep[0] * nstep[1] * nstep[2];
+    DevBuf dr(sizeof(double) * np), dg(sizeof(double) * np);
+    int rc = c2g_nciplot_dev(hp, x0, xmat, nstep, prec, dr.as<double>(), dg.as<double>(), nullptr, stats);
+    if (rc != C2G_OK) fail(rc, g_last_error);
+    C2G_CUDA(cudaMemcpy(crho, dr.p, sizeof(double) * np, cudaMemcpyDeviceToHost));
+    C2G_CUDA(cudaMemcpy(cgrad, dg.p, sizeof(double) * np, cudaMemcpyDeviceToHost));
+  });
+}
+
+}  // extern "C"

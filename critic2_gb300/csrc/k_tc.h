@@ -1,0 +1,26 @@
+// Split-precision (tcgen05 tensor-core) evaluator: internal interface.
+#pragma once
+
+#include "c2g_internal.h"
+
+namespace c2g {
+
+// Builds the split operands of the coefficient matrix on the device.
+TcOperands *tc_create(Handle &h);
+void tc_destroy(TcOperands *t);
+
+// kRecNci records (rho, grad, hess) at n device points, split precision.
+void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st);
+
+// kRecNci records of the points x(3, idx[t]), t < *d_count (<= maxn), split
+// precision, written at rec[t].
+void tc_points_index(Handle &h, int prec, const double *d_x, const int *d_idx, const int *d_count,
+                     int maxn, double *d_rec, cudaStream_t st);
+
+// NCI grid in split precision followed by the FP64 re-check of the points
+// whose Hessian has |lambda2| < 1e-3 |lambda1|.  Records ev_split after the
+// split pass when not null.  Returns the number of re-checked points.
+long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad,
+                 cudaStream_t st, cudaEvent_t ev_split);
+
+}  // namespace c2g

@@ -1,0 +1,268 @@
+"""Seeded synthetic molecular wavefunctions for the evaluator's workloads.
+
+The generator builds molecules made of Cartesian Gaussian primitives centred
+on atoms, with MO coefficients in the wfx convention (coefficients multiply
+*unnormalised* primitives, as `read_wfx` stores them;
+src/wfn_private@proc.F90:1121-1284 applies no normalisation for wfx files).
+
+Primitive types follow critic2's `li(3,56)` exponent table
+(src/wfn_private@proc.F90:3186-3196): type 1 = s; 2-4 = x,y,z; 5-10 =
+xx,yy,zz,xy,xz,yz; 11-20 = xxx,yyy,zzz,xxy,xxz,yyz,xyy,xzz,yzz,xyz.
+
+Arrays use critic2's memory layout: `cmo` has shape (npri, nmo) in C order,
+which is Fortran's `cmo(nmoocc, npri)` (MO index fastest).  `icenter` and
+`itype` are 1-based, exactly as read from a wfx file.
+
+Workloads (all coordinates in bohr):
+
+  nci12     12 atoms (8 H + 4 of C/N/O) as a 2-fragment complex in a
+            12-bohr box, ~150 primitives (heavy: 6 s, 3 p, 1 d shells;
+            H: 5 s, 1 p), 12 occupied MOs, 80^3 NCI grid at 0.1 bohr.
+  nci60     60 atoms, ~1200 primitives (s/p/d), 120 MOs, 200^3 grid.
+  prec200   200 atoms, ~4000 primitives (s/p/d/f; f exponents 0.3-5),
+            400 MOs, 256^3 grid.
+  cp100     100 atoms, ~2000 primitives (s/p/d), 200 MOs; CP search and a
+            64^3 coarse density grid.
+  large500  500 atoms, ~10000 primitives (s/p/d/f), 1000 MOs, 320^3 grid.
+
+Boxes grow with the atom count at the density of the 12-atom case
+(12 atoms per 12^3 bohr^3).  Atoms keep a minimum separation of 1.8 bohr.
+The share of hydrogens (which get the reduced 5s1p shell set) is chosen so
+that the primitive count meets the stated total.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Dict, List, Optional
+
+import numpy as np
+
+# critic2 li(3,56) table restricted to s..f (rows 1-20), 1-based type index.
+LI = np.array([
+    (0, 0, 0),
+    (1, 0, 0), (0, 1, 0), (0, 0, 1),
+    (2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1),
+    (3, 0, 0), (0, 3, 0), (0, 0, 3), (2, 1, 0), (2, 0, 1), (0, 2, 1),
+    (1, 2, 0), (1, 0, 2), (0, 1, 2), (1, 1, 1),
+], dtype=np.int32)
+
+SHELL_TYPES = {"s": [1], "p": [2, 3, 4], "d": list(range(5, 11)), "f": list(range(11, 21))}
+HEAVY_Z = (6, 7, 8)
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    natom: int
+    target_npri: Optional[int]
+    nh: Optional[int]
+    with_f: bool
+    nmo: int
+    grid: int            # grid points per axis (0 = no NCI grid)
+    step: float          # grid step (bohr)
+    fragments: int
+    seed: int
+    coarse: int = 0      # coarse density grid for the CP-seed proposer
+
+
+WORKLOADS: Dict[str, Workload] = {
+    "nci12": Workload("nci12", 12, None, 8, False, 12, 80, 0.1, 2, 1),
+    "nci60": Workload("nci60", 60, 1200, None, False, 120, 200, 0.1, 1, 2),
+    "prec200": Workload("prec200", 200, 4000, None, True, 400, 256, 0.1, 1, 3),
+    "cp100": Workload("cp100", 100, 2000, None, False, 200, 0, 0.1, 1, 4, coarse=64),
+    "large500": Workload("large500", 500, 10000, None, True, 1000, 320, 0.1, 1, 5),
+}
+
+
+@dataclasses.dataclass
+class Molecule:
+    """A molecular wavefunction in critic2's molwfn layout (see module doc)."""
+    atom_xyz: np.ndarray     # (natom, 3) float64, bohr
+    atom_z: np.ndarray       # (natom,) int32
+    icenter: np.ndarray      # (npri,) int32, 1-based
+    itype: np.ndarray        # (npri,) int32, 1-based li index
+    e: np.ndarray            # (npri,) float64
+    occ: np.ndarray          # (nmo,) float64
+    cmo: np.ndarray          # (npri, nmo) float64, C order == Fortran cmo(nmo,npri)
+    wfntyp: int = 0          # 0 rhf, 1 uhf, 2 rohf, 3 frac
+    nalpha: int = 0
+    name: str = ""
+
+    @property
+    def natom(self) -> int:
+        return int(self.atom_xyz.shape[0])
+
+    @property
+    def npri(self) -> int:
+        return int(self.e.shape[0])
+
+    @property
+    def nmo(self) -> int:
+        return int(self.occ.shape[0])
+
+
+def _shells(heavy: bool, with_f: bool) -> List[str]:
+    if heavy:
+        sh = ["s"] * 6 + ["p"] * 3 + ["d"]
+        if with_f:
+            sh.append("f")
+        return sh
+    return ["s"] * 5 + ["p"]
+
+
+def _nprim(shells: List[str]) -> int:
+    return sum(len(SHELL_TYPES[s]) for s in shells)
+
+
+def _place_atoms(rng, natom: int, box: float, fragments: int, dmin: float = 1.8) -> np.ndarray:
+    pos = np.zeros((natom, 3))
+    n = 0
+    gap = 0.75
+    tries = 0
+    while n < natom:
+        tries += 1
+        if tries > 2_000_000:
+            raise RuntimeError("atom placement failed")
+        x = rng.uniform(0.0, box, size=3)
+        if fragments == 2:
+            # first half of the atoms in the left slab, second half in the right slab
+            if n < natom // 2:
+                x[0] = rng.uniform(0.0, box / 2 - gap)
+            else:
+                x[0] = rng.uniform(box / 2 + gap, box)
+        if n and np.min(np.sum((pos[:n] - x) ** 2, axis=1)) < dmin * dmin:
+            continue
+        pos[n] = x
+        n += 1
+    return pos
+
+
+def make_molecule(name: str, seed: Optional[int] = None) -> Molecule:
+    """Builds the named workload's molecule (deterministic for a given seed)."""
+    w = WORKLOADS[name]
+    rng = np.random.default_rng(w.seed if seed is None else seed)
+    per_heavy = _nprim(_shells(True, w.with_f))
+    per_h = _nprim(_shells(False, w.with_f))
+    if w.nh is not None:
+        nh = w.nh
+    else:
+        nh = int(round(w.natom * (per_heavy - w.target_npri / w.natom) / (per_heavy - per_h)))
+        nh = max(0, min(w.natom, nh))
+    box = 12.0 * (w.natom / 12.0) ** (1.0 / 3.0)
+    pos = _place_atoms(rng, w.natom, box, w.fragments)
+    # which atoms are H: spread over both fragments
+    isH = np.zeros(w.natom, dtype=bool)
+    isH[rng.permutation(w.natom)[:nh]] = True
+    if w.fragments == 2:
+        half = w.natom // 2
+        isH[:] = False
+        isH[rng.permutation(half)[: nh // 2]] = True
+        isH[half + rng.permutation(w.natom - half)[: nh - nh // 2]] = True
+    z = np.where(isH, 1, rng.choice(HEAVY_Z, size=w.natom)).astype(np.int32)
+
+    icenter, itype, e = [], [], []
+    for a in range(w.natom):
+        for sh in _shells(not isH[a], w.with_f):
+            if sh == "f":
+                alpha = math.exp(rng.uniform(math.log(0.3), math.log(5.0)))
+            else:
+                alpha = math.exp(rng.uniform(math.log(0.1), math.log(50.0)))
+            for t in SHELL_TYPES[sh]:
+                icenter.append(a + 1)
+                itype.append(t)
+                e.append(alpha)
+    npri = len(e)
+    cmo = rng.standard_normal((npri, w.nmo))
+    occ = np.full(w.nmo, 2.0)
+    return Molecule(pos, z, np.array(icenter, np.int32), np.array(itype, np.int32),
+                    np.array(e, np.float64), occ, np.ascontiguousarray(cmo),
+                    wfntyp=0, nalpha=w.nmo, name=name)
+
+
+def nci_grid(mol: Molecule, n: int, step: float):
+    """NCI grid geometry in critic2's form (src/nci@proc.f90:430-447).
+
+    For a molecule with explicit limits critic2 uses a diagonal xmat of the
+    step and nstep points per axis.  The grid here has n points per axis at
+    the given step, centred on the centre of the molecule's bounding box.
+    Returns (x0[3], xmat[3,3] with columns = axis steps, nstep[3]).
+    """
+    lo = mol.atom_xyz.min(axis=0)
+    hi = mol.atom_xyz.max(axis=0)
+    c = 0.5 * (lo + hi)
+    x0 = c - 0.5 * step * (n - 1)
+    xmat = np.diag([step, step, step]).astype(np.float64)
+    return x0.astype(np.float64), xmat, np.array([n, n, n], np.int32)
+
+
+def grid_points(x0, xmat, nstep, i_range=None) -> np.ndarray:
+    """Cartesian coordinates of grid points in critic2's (k,j,i) order (k fastest).
+
+    x = x0 + i*xmat[:,0] + j*xmat[:,1] + k*xmat[:,2]   (src/nci@proc.f90:548)
+    Returns an array of shape (n_i, n2, n3, 3).
+    """
+    n1, n2, n3 = (int(v) for v in nstep)
+    i0, i1 = (0, n1) if i_range is None else i_range
+    ii = np.arange(i0, i1, dtype=np.float64)
+    jj = np.arange(n2, dtype=np.float64)
+    kk = np.arange(n3, dtype=np.float64)
+    xm = np.asarray(xmat, np.float64)
+    pts = (np.asarray(x0)[None, None, None, :]
+           + ii[:, None, None, None] * xm[:, 0]
+           + jj[None, :, None, None] * xm[:, 1]
+           + kk[None, None, :, None] * xm[:, 2])
+    return pts
+
+
+def write_wfx(mol: Molecule, path: str) -> None:
+    """Writes the molecule as a wfx file readable by critic2's read_wfx.
+
+    The MO coefficient block follows the structure read_wfx parses
+    (src/wfn_private@proc.F90:1215-1221): one skipped line after the section
+    tag, then per MO two skipped lines and the reals, which end at the next
+    line that starts with '<'.
+    """
+    def block(tag, values, fmt):
+        lines = [f"<{tag}>"]
+        for i in range(0, len(values), 5):
+            lines.append(" " + " ".join(fmt(v) for v in values[i:i + 5]))
+        lines.append(f"</{tag}>")
+        return lines
+
+    out = ["<Title>", f" synthetic {mol.name}", "</Title>",
+           "<Keywords>", " GTO", "</Keywords>",
+           "<Number of Nuclei>", f" {mol.natom}", "</Number of Nuclei>",
+           "<Number of Occupied Molecular Orbitals>", f" {mol.nmo}",
+           "</Number of Occupied Molecular Orbitals>",
+           "<Number of Perturbations>", " 0", "</Number of Perturbations>",
+           "<Net Charge>", " 0", "</Net Charge>",
+           "<Electronic Spin Multiplicity>", " 1", "</Electronic Spin Multiplicity>",
+           "<Number of Alpha Electrons>", f" {mol.nalpha}", "</Number of Alpha Electrons>",
+           "<Number of Beta Electrons>", f" {mol.nalpha}", "</Number of Beta Electrons>",
+           "<Nuclear Names>"]
+    sym = {1: "H", 6: "C", 7: "N", 8: "O"}
+    for a in range(mol.natom):
+        out.append(f" {sym.get(int(mol.atom_z[a]), 'X')}{a + 1}")
+    out.append("</Nuclear Names>")
+    out += block("Atomic Numbers", [int(v) for v in mol.atom_z], lambda v: f"{v:d}")
+    out += block("Nuclear Charges", [float(v) for v in mol.atom_z], lambda v: f"{v:.12E}")
+    out.append("<Nuclear Cartesian Coordinates>")
+    for a in range(mol.natom):
+        out.append(" " + " ".join(f"{v: .16E}" for v in mol.atom_xyz[a]))
+    out.append("</Nuclear Cartesian Coordinates>")
+    out += ["<Number of Primitives>", f" {mol.npri}", "</Number of Primitives>"]
+    out += block("Primitive Centers", [int(v) for v in mol.icenter], lambda v: f"{v:d}")
+    out += block("Primitive Types", [int(v) for v in mol.itype], lambda v: f"{v:d}")
+    out += block("Primitive Exponents", [float(v) for v in mol.e], lambda v: f"{v:.16E}")
+    out += block("Molecular Orbital Occupation Numbers", [float(v) for v in mol.occ],
+                 lambda v: f"{v:.16E}")
+    out.append("<Molecular Orbital Primitive Coefficients>")
+    for m in range(mol.nmo):
+        out += ["<MO Number>", f" {m + 1}", "</MO Number>"]
+        col = mol.cmo[:, m]
+        for i in range(0, mol.npri, 4):
+            out.append(" " + " ".join(f"{v: .16E}" for v in col[i:i + 4]))
+    out.append("</Molecular Orbital Primitive Coefficients>")
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")

@@ -1,0 +1,153 @@
+"""Host mirror of critic2's molecular-wavefunction field API over the C ABI.
+
+`Wavefunction` plays the role of critic2's `molwfn` plus the wavefunction
+branch of `field` (src/wfn_private.f90:91-141, src/fieldmod.f90:178-269):
+`rho2` is molwfn%rho2 for a batch of points, `grd` is field%grd, `newton`
+is field%newton for a batch of seeds; `nciplot` and `autocritic` are the
+two consumers the reference drives from them (src/nci@proc.f90:540-605,
+src/autocp@proc.f90:755-822).  Every call goes to the GPU library; there is
+no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _prec(p) -> int:
+    if isinstance(p, str):
+        return L.PREC[p]
+    return int(p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Wavefunction:
+    """A molecular wavefunction resident on the GPU."""
+
+    def __init__(self, mol=None, *, _handle=None):
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            lib = L.lib()
+            L.check(lib.c2g_wfn_create(
+                mol.natom, _f64(mol.atom_xyz.reshape(-1)), _i32(mol.atom_z), mol.npri, mol.nmo,
+                _i32(mol.icenter), _i32(mol.itype), _f64(mol.e), _f64(mol.occ),
+                _f64(mol.cmo.reshape(-1)), int(mol.wfntyp), int(mol.nalpha), C.byref(self._h)))
+        n = [C.c_int() for _ in range(5)]
+        L.check(L.lib().c2g_wfn_info(self._h, *[C.byref(v) for v in n]))
+        self.natom, self.npri, self.nmo, self.wfntyp, self.nalpha = (v.value for v in n)
+
+    @classmethod
+    def from_wfx(cls, path: str) -> "Wavefunction":
+        h = C.c_void_p()
+        L.check(L.lib().c2g_wfn_read_wfx(path.encode(), C.byref(h)))
+        return cls(_handle=h)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            L.lib().c2g_wfn_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------ rho2/grd
+    def rho2(self, xyz, nder: int = 2, prec="fp64") -> dict:
+        """molwfn%rho2 at points xyz (n,3).  Arrays are per point:
+        rho (n,3) total/up/down; grad (n,3,3) [spin][xyz]; hess (n,3,3,3)
+        [spin][col][row]; gkin (n,3); stress (n,3,3); vir (n,)."""
+        x = _f64(xyz).reshape(-1, 3)
+        n = x.shape[0]
+        out = dict(rho=np.zeros((n, 3)), grad=np.zeros((n, 3, 3)), hess=np.zeros((n, 3, 3, 3)),
+                   gkin=np.zeros((n, 3)), stress=np.zeros((n, 3, 3)), vir=np.zeros(n))
+        L.check(L.lib().c2g_rho2(self._h, n, L.ptr(x), nder, _prec(prec), L.ptr(out["rho"]),
+                                 L.ptr(out["grad"]), L.ptr(out["hess"]), L.ptr(out["gkin"]),
+                                 L.ptr(out["stress"]), L.ptr(out["vir"])))
+        return out
+
+    def grd(self, xyz, nder: int = 2, prec="fp64") -> dict:
+        """field%grd at points xyz (n,3): f, gf (n,3), gfmod, hf (n,3,3),
+        hfeval (n,3) ascending, r, s, isnuc."""
+        x = _f64(xyz).reshape(-1, 3)
+        n = x.shape[0]
+        o = dict(f=np.zeros(n), gf=np.zeros((n, 3)), gfmod=np.zeros(n), hf=np.zeros((n, 3, 3)),
+                 hfeval=np.zeros((n, 3)), r=np.zeros(n, np.int32), s=np.zeros(n, np.int32),
+                 isnuc=np.zeros(n, np.int32))
+        L.check(L.lib().c2g_grd(self._h, n, L.ptr(x), nder, _prec(prec), L.ptr(o["f"]),
+                                L.ptr(o["gf"]), L.ptr(o["gfmod"]), L.ptr(o["hf"]),
+                                L.ptr(o["hfeval"]), L.ptr(o["r"]), L.ptr(o["s"]),
+                                L.ptr(o["isnuc"])))
+        return o
+
+    # ---------------------------------------------------------------- NCI
+    def nciplot(self, x0, xmat, nstep, prec="fp64"):
+        """NCI grid: returns crho, cgrad as (n1, n2, n3) arrays (Fortran
+        (k,j,i) order, k fastest) and the stats record.  xmat[:, i] is the
+        step of axis i."""
+        nstep = _i32(nstep)
+        shape = tuple(int(v) for v in nstep)
+        crho, cgrad = np.zeros(shape), np.zeros(shape)
+        st = L.NciStats()
+        xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+        L.check(L.lib().c2g_nciplot(self._h, _f64(x0), xm, nstep, _prec(prec), L.ptr(crho),
+                                    L.ptr(cgrad), C.byref(st)))
+        return crho, cgrad, st
+
+    def nciplot_dev(self, x0, xmat, nstep, prec, d_crho: int, d_cgrad: int, stream: int = 0,
+                    stats: bool = False):
+        """NCI grid into device buffers (raw pointers), on a CUDA stream."""
+        st = L.NciStats()
+        xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+        L.check(L.lib().c2g_nciplot_dev(self._h, _f64(x0), xm, _i32(nstep), _prec(prec),
+                                        C.c_void_p(d_crho), C.c_void_p(d_cgrad),
+                                        C.c_void_p(stream), C.byref(st) if stats else None))
+        return st
+
+    # -------------------------------------------------------------- Newton
+    def newton(self, xyz, gfnormeps: float = 1e-12, maxit: int = 200, prec="fp64"):
+        x = _f64(xyz).reshape(-1, 3).copy()
+        ier = np.zeros(x.shape[0], np.int32)
+        L.check(L.lib().c2g_newton(self._h, x.shape[0], L.ptr(x), gfnormeps, maxit, _prec(prec),
+                                   L.ptr(ier)))
+        return x, ier
+
+    def pair_seeds(self, maxdist: float = 15.0, npts: int = 5) -> np.ndarray:
+        n = C.c_int(0)
+        L.check(L.lib().c2g_pair_seeds(self._h, maxdist, npts, None, C.byref(n)))
+        buf = np.zeros((max(n.value, 1), 3))
+        L.check(L.lib().c2g_pair_seeds(self._h, maxdist, npts, L.ptr(buf), C.byref(n)))
+        return buf[: n.value]
+
+    def autocritic(self, seeds: Optional[np.ndarray] = None, prec="fp64") -> dict:
+        s = None if seeds is None else _f64(seeds).reshape(-1, 3)
+        ns = 0 if s is None else s.shape[0]
+        maxcp = self.natom + (ns if s is not None else max(1, len(self.pair_seeds()))) + 1
+        xyz, typ, f = np.zeros((maxcp, 3)), np.zeros(maxcp, np.int32), np.zeros(maxcp)
+        rep = L.CpReport()
+        L.check(L.lib().c2g_autocritic(self._h, ns, L.ptr(s), _prec(prec), maxcp, L.ptr(xyz),
+                                       L.ptr(typ), L.ptr(f), C.byref(rep)))
+        n = rep.ncp
+        return dict(xyz=xyz[:n], typ=typ[:n], f=f[:n], counts=np.array(rep.count[:]),
+                    ph=rep.poincare_hopf, nseed=rep.nseed, nconverged=rep.nconverged,
+                    ms=rep.ms_total)

@@ -1,0 +1,177 @@
+/*
+ * critic2_gb300 -- C ABI of the GB300 molecular-wavefunction field evaluator.
+ *
+ * The library evaluates critic2's GTO molecular-wavefunction field (density,
+ * gradient, Hessian and derived quantities) on one GPU and runs the two
+ * consumers of that evaluator that critic2 drives from it: the NCI grid
+ * (reduced density gradient s and sign(lambda2)*rho) and the AUTO Newton
+ * critical-point search.
+ *
+ * Conventions (identical to critic2's internal ones):
+ *   - Cartesian coordinates in bohr, in the frame of the wavefunction file.
+ *   - Arrays are Fortran-ordered where critic2 passes Fortran arrays:
+ *     cmo is cmo(nmo, npri) (MO index fastest), a 3x3 matrix is column-major,
+ *     a batch of n points is xyz(3, n).
+ *   - icenter and itype are 1-based, itype indexes critic2's li(3,56) table.
+ *   - Every entry point returns an int status (C2G_OK = 0).  No exception
+ *     crosses the ABI; c2g_last_error() gives the calling thread's message.
+ *   - A handle may be used by one host thread at a time.
+ *
+ * Reference interfaces replaced (paths within the critic2 source tree):
+ *   c2g_wfn_create / c2g_wfn_read_wfx : molwfn%read_wfx + prune_primitives +
+ *       complete_struct (src/wfn_private@proc.F90:1121-1284, 3632-3785)
+ *   c2g_rho2      : molwfn%rho2 (src/wfn_private.f90:293-307,
+ *                   src/wfn_private@proc.F90:2484-2705), batched over points
+ *   c2g_grd       : field%grd for a wavefunction field
+ *                   (src/fieldmod.f90:178-184, src/fieldmod@proc.f90:808-1171)
+ *   c2g_nciplot   : the nciplot grid loop (src/nci@proc.f90:540-605)
+ *   c2g_newton    : field%newton (src/fieldmod.f90:264-269,
+ *                   src/fieldmod@proc.f90:2238-2279), batched over seeds
+ *   c2g_autocritic: autocritic's seed / Newton / addcp / sortcps core
+ *                   (src/autocp@proc.f90:423-437, 755-822,
+ *                   src/fieldmod@proc.f90:2288-2466)
+ */
+#ifndef CRITIC2_GB300_H
+#define CRITIC2_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define C2G_ABI_VERSION 1
+
+/* status codes */
+#define C2G_OK 0
+#define C2G_ERR_ARG 1         /* bad argument (null pointer, size, mode) */
+#define C2G_ERR_CUDA 2        /* a CUDA call failed, or no usable GPU */
+#define C2G_ERR_ALLOC 3       /* host or device allocation failed */
+#define C2G_ERR_IO 4          /* file could not be read or parsed */
+#define C2G_ERR_UNSUPPORTED 5 /* valid request this build does not support */
+
+/* arithmetic of the evaluation */
+#define C2G_PREC_FP64 0   /* FP64 everywhere (the plain form) */
+#define C2G_PREC_TF32X3 1 /* TF32 split (3 products), FP32 accumulation */
+#define C2G_PREC_BF16X3 2 /* BF16 split (3 products), FP32 accumulation */
+
+/* wavefunction types (src/wfn_private.f90:156-159) */
+#define C2G_WFN_RHF 0
+#define C2G_WFN_UHF 1
+#define C2G_WFN_ROHF 2
+#define C2G_WFN_FRAC 3
+
+typedef struct c2g_wfn c2g_wfn;
+
+/* Library ABI version (C2G_ABI_VERSION). */
+int c2g_abi_version(void);
+
+/* Message of the last failed call on this host thread (always NUL-ended).
+ * Returns the length of the full message. */
+int c2g_last_error(char *buf, int len);
+
+/* Creates a wavefunction handle from molwfn arrays.  The arrays are copied
+ * (the caller keeps ownership); duplicate primitives are merged and the
+ * primitive cutoffs computed exactly as critic2's prune_primitives and
+ * complete_struct do; the result is uploaded to the current CUDA device.
+ *   atom_xyz(3,natom), atom_z(natom): nuclei (atomic numbers; 1 = H)
+ *   icenter(npri), itype(npri): 1-based centre and li type (1..56)
+ *   e(npri): exponents; occ(nmo): occupations; cmo(nmo,npri): coefficients
+ *   wfntyp: C2G_WFN_*; nalpha: number of alpha MOs (UHF/ROHF split)
+ * Replaces src/wfn_private@proc.F90:3632-3785 (prune_primitives,
+ * complete_struct) following read_wfx. */
+int c2g_wfn_create(int natom, const double *atom_xyz, const int *atom_z, int npri, int nmo,
+                   const int *icenter, const int *itype, const double *e, const double *occ,
+                   const double *cmo, int wfntyp, int nalpha, c2g_wfn **out);
+
+/* Reads a wfx file (nuclei, primitives, occupied MOs) like critic2's
+ * `molecule file.wfx` + `load file.wfx` and creates a handle.  Replaces
+ * read_wfx, src/wfn_private@proc.F90:1121-1284. */
+int c2g_wfn_read_wfx(const char *path, c2g_wfn **out);
+
+/* Frees the handle and its device memory. */
+int c2g_wfn_destroy(c2g_wfn *h);
+
+/* Sizes after pruning. */
+int c2g_wfn_info(const c2g_wfn *h, int *natom, int *npri, int *nmo, int *wfntyp, int *nalpha);
+
+/* molwfn%rho2 over a batch of n points (src/wfn_private@proc.F90:2484-2705).
+ * xyz(3,n).  Outputs (any may be NULL; nder >= the order each needs):
+ *   rho(3,n)      total, up, down density
+ *   grad(3,3,n)   gradient per spin channel (columns total, up, down)  [nder>=1]
+ *   hess(3,3,3,n) Hessian per spin channel                             [nder>=2]
+ *   gkin(3,n)     kinetic energy density G per spin channel            [nder>=1]
+ *   stress(3,3,n) Schrodinger stress tensor; vir(n) its trace          [nder>=2]
+ * prec: C2G_PREC_FP64 gives every output; the split modes give rho, grad
+ * and hess totals only (spin channels are then the RHF halves). */
+int c2g_rho2(c2g_wfn *h, int n, const double *xyz, int nder, int prec, double *rho,
+             double *grad, double *hess, double *gkin, double *stress, double *vir);
+
+/* field%grd for the wavefunction field at n points: molecular-cell wrap,
+ * rho2, nucleus check (|grad| := 0 within 1e-5 bohr of a nucleus),
+ * Hessian eigenvalues (ascending), rank r and signature s with the 1e-8
+ * degeneracy threshold (src/fieldmod@proc.f90:808-1171).  Outputs may be
+ * NULL: f(n), gf(3,n), gfmod(n), hf(3,3,n), hfeval(3,n), r(n), s(n),
+ * isnuc(n). */
+int c2g_grd(c2g_wfn *h, int n, const double *xyz, int nder, int prec, double *f, double *gf,
+            double *gfmod, double *hf, double *hfeval, int *r, int *s, int *isnuc);
+
+/* Error statistics of a split-precision NCI evaluation, filled when the
+ * caller asks for an FP64 re-check (see c2g_nciplot). */
+typedef struct {
+  long npoints;
+  long nrecheck;        /* points re-evaluated in FP64 (|l2| < 1e-3 |l1|) */
+  double ms_kernel;     /* device time of the evaluation, milliseconds */
+  double ms_recheck;    /* device time of the FP64 re-check pass */
+} c2g_nci_stats;
+
+/* The nciplot grid loop (src/nci@proc.f90:540-605) over the grid
+ * x = x0 + i*xmat(:,1) + j*xmat(:,2) + k*xmat(:,3), i < nstep(1), j <
+ * nstep(2), k < nstep(3).  Writes crho(k,j,i) = sign(rho, lambda2)*100 and
+ * cgrad(k,j,i) = s (k fastest), host arrays of nstep(1)*nstep(2)*nstep(3)
+ * doubles.  xmat is column-major (column i = step vector of axis i).
+ * In the split modes the points whose Hessian eigenvalues satisfy
+ * |lambda2| < 1e-3 |lambda1| are re-evaluated in FP64.  stats may be NULL. */
+int c2g_nciplot(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec,
+                double *crho, double *cgrad, c2g_nci_stats *stats);
+
+/* As c2g_nciplot, writing device arrays on the given CUDA stream (NULL =
+ * legacy default stream).  Returns after the work is enqueued and, when
+ * stats is not NULL, after it finishes. */
+int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep,
+                    int prec, double *d_crho, double *d_cgrad, void *stream,
+                    c2g_nci_stats *stats);
+
+/* field%newton for n seeds at once (src/fieldmod@proc.f90:2238-2279):
+ * xyz(3,n) in/out; ier(n): 0 converged (|grad| < gfnormeps), 1 invalid or
+ * singular Hessian, 2 maxit reached.  In the split modes the iterations run
+ * in split precision until |grad| < 1e-5 and finish in FP64. */
+int c2g_newton(c2g_wfn *h, int n, double *xyz, double gfnormeps, int maxit, int prec, int *ier);
+
+/* Default molecular pair seeds of critic2's AUTO (src/autocp@proc.f90:
+ * 423-437, 665-729): for every ordered atom pair closer than maxdist, npts
+ * points at fractions k/(npts+1), filtered by the molecular-cell border.
+ * With xseed NULL returns the count in *nseed; otherwise writes up to
+ * *nseed seeds xseed(3,*) and sets *nseed to the number written. */
+int c2g_pair_seeds(const c2g_wfn *h, double maxdist, int npts, double *xseed, int *nseed);
+
+/* CP list result of c2g_autocritic. */
+typedef struct {
+  int ncp;              /* CPs written (nuclei first, then sortcps order) */
+  int count[4];         /* n, b, r, c */
+  int poincare_hopf;    /* n - b + r - c (1 for a molecule) */
+  int nseed;            /* seeds searched */
+  int nconverged;       /* Newton runs with ier == 0 */
+  double ms_total;      /* wall time of the search, milliseconds */
+} c2g_cp_report;
+
+/* autocritic core: Newton from every seed (c2g_newton), addcp on the
+ * converged ones (cpeps 1e-2, nuceps 0.1, nucepsh 0.2, gradient check
+ * max(1e-4, gfnormeps), degenerate CPs dropped), sortcps.  Outputs up to
+ * maxcp CPs: cp_xyz(3,*), cp_typ(*) (signature: -3 n, -1 b, 1 r, 3 c),
+ * cp_f(*) density.  With xseed NULL the default pair seeds are used. */
+int c2g_autocritic(c2g_wfn *h, int nseed, const double *xseed, int prec, int maxcp,
+                   double *cp_xyz, int *cp_typ, double *cp_f, c2g_cp_report *report);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,725 @@
+/*
+ * CPU oracle for the critic2 molecular-wavefunction evaluator path.
+ * TEST INFRASTRUCTURE ONLY: see oracle.h for its role and parity status.
+ *
+ * Each function restates the reference routine cited in its comment
+ * (paths relative to the critic2 source tree).
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Cartesian exponent table, critic2 li(3,56) order
+ * (src/wfn_private@proc.F90:3186-3196): s; p; d; f; g; h. */
+static const int LI[56][3] = {
+    {0, 0, 0},
+    {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+    {2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1},
+    {3, 0, 0}, {0, 3, 0}, {0, 0, 3}, {2, 1, 0}, {2, 0, 1}, {0, 2, 1},
+    {1, 2, 0}, {1, 0, 2}, {0, 1, 2}, {1, 1, 1},
+    {4, 0, 0}, {0, 4, 0}, {0, 0, 4}, {3, 1, 0}, {3, 0, 1}, {1, 3, 0}, {0, 3, 1}, {1, 0, 3},
+    {0, 1, 3}, {2, 2, 0}, {2, 0, 2}, {0, 2, 2}, {2, 1, 1}, {1, 2, 1}, {1, 1, 2},
+    {0, 0, 5}, {0, 1, 4}, {0, 2, 3}, {0, 3, 2}, {0, 4, 1}, {0, 5, 0}, {1, 0, 4}, {1, 1, 3},
+    {1, 2, 2}, {1, 3, 1}, {1, 4, 0}, {2, 0, 3}, {2, 1, 2}, {2, 2, 1}, {2, 3, 0}, {3, 0, 2},
+    {3, 1, 1}, {3, 2, 0}, {4, 0, 1}, {4, 1, 0}, {5, 0, 0}};
+
+#define RPRIM_THRES 1e-12   /* src/wfn_private@proc.F90:170 */
+#define VSMALL 1e-80        /* src/param.F90:27 */
+#define FLOOREPS 1e-4       /* src/fieldmod@proc.f90:31 */
+#define BOHRTOA 0.52917720859 /* src/param.F90:42 */
+#define CP_HDEGEN 1e-8      /* src/global.f90:149 */
+
+struct owfn {
+  int natom;
+  double *xyz;
+  int *z;
+  int npri, nmo;
+  int *icenter; /* 0-based */
+  int *itype;   /* 1-based li index */
+  double *e, *occ, *cmo;
+  int wfntyp, nalpha;
+  double *dran, *spcutoff;
+  int *lmax, *icord, *iprilo, *iprihi;
+  double cell_lo[3], aa[3], molborder[3];
+};
+
+static int limax_of(int itype) {
+  const int *l = LI[itype - 1];
+  int m = l[0] > l[1] ? l[0] : l[1];
+  return m > l[2] ? m : l[2];
+}
+
+/* stable index sort by a double key (insertion into merge sort) */
+static void msort_idx(int *idx, int n, const double *key, int *tmp) {
+  if (n < 2) return;
+  int h = n / 2;
+  msort_idx(idx, h, key, tmp);
+  msort_idx(idx + h, n - h, key, tmp);
+  int i = 0, j = h, k = 0;
+  while (i < h && j < n) tmp[k++] = (key[idx[j]] < key[idx[i]]) ? idx[j++] : idx[i++];
+  while (i < h) tmp[k++] = idx[i++];
+  while (j < n) tmp[k++] = idx[j++];
+  memcpy(idx, tmp, sizeof(int) * n);
+}
+
+/* prune_primitives, src/wfn_private@proc.F90:3632-3684: merge primitives with
+ * the same exponent (within 1e-12), type and centre, summing their MO
+ * coefficient columns, then compact the arrays keeping the original order. */
+static void prune_primitives(owfn *w) {
+  int n = w->npri;
+  int *iord = malloc(sizeof(int) * n), *tmp = malloc(sizeof(int) * n);
+  char *keep = malloc(n);
+  for (int i = 0; i < n; i++) iord[i] = i, keep[i] = 1;
+  msort_idx(iord, n, w->e, tmp);
+  for (int i = 0; i < n; i++) {
+    int a = iord[i];
+    if (!keep[a]) continue;
+    for (int j = i + 1; j < n; j++) {
+      int b = iord[j];
+      if (fabs(w->e[b] - w->e[a]) > 1e-12) continue;
+      if (w->itype[a] == w->itype[b] && w->icenter[a] == w->icenter[b] && keep[b]) {
+        for (int m = 0; m < w->nmo; m++) w->cmo[(size_t)a * w->nmo + m] += w->cmo[(size_t)b * w->nmo + m];
+        keep[b] = 0;
+      }
+    }
+  }
+  int j = 0;
+  for (int i = 0; i < n; i++) {
+    if (!keep[i]) continue;
+    if (j != i) {
+      memmove(w->cmo + (size_t)j * w->nmo, w->cmo + (size_t)i * w->nmo, sizeof(double) * w->nmo);
+      w->e[j] = w->e[i];
+      w->icenter[j] = w->icenter[i];
+      w->itype[j] = w->itype[i];
+    }
+    j++;
+  }
+  w->npri = j;
+  free(iord);
+  free(tmp);
+  free(keep);
+}
+
+/* complete_struct, src/wfn_private@proc.F90:3692-3785 (GTO branch):
+ * dran = sqrt(-ln(thres)/alpha), per-atom cutoff = max dran, per-atom lmax
+ * (largest single Cartesian exponent), primitives ordered by centre. */
+static void complete_struct(owfn *w) {
+  int n = w->npri, na = w->natom;
+  w->dran = malloc(sizeof(double) * n);
+  w->spcutoff = calloc(na, sizeof(double));
+  w->lmax = calloc(na, sizeof(int));
+  w->icord = malloc(sizeof(int) * n);
+  w->iprilo = malloc(sizeof(int) * na);
+  w->iprihi = malloc(sizeof(int) * na);
+  for (int i = 0; i < n; i++) {
+    w->dran[i] = sqrt(-log(RPRIM_THRES) / w->e[i]);
+    int a = w->icenter[i];
+    if (w->dran[i] > w->spcutoff[a]) w->spcutoff[a] = w->dran[i];
+    int lm = limax_of(w->itype[i]);
+    if (lm > w->lmax[a]) w->lmax[a] = lm;
+  }
+  /* stable sort by centre */
+  int k = 0;
+  for (int a = 0; a < na; a++) {
+    w->iprilo[a] = -1;
+    w->iprihi[a] = -2;
+    for (int i = 0; i < n; i++)
+      if (w->icenter[i] == a) {
+        if (w->iprilo[a] < 0) w->iprilo[a] = k;
+        w->iprihi[a] = k;
+        w->icord[k++] = i;
+      }
+  }
+}
+
+/* Molecular cell (src/crystalmod@proc.f90:222-249, 545): bounding box of the
+ * atoms grown by the default border (10 angstrom, src/global.f90:122); the
+ * inner region that keeps CPs is the cell minus molborder on each side. */
+static void molecular_cell(owfn *w) {
+  double border = 10.0 / BOHRTOA;
+  for (int j = 0; j < 3; j++) {
+    double lo = 1e40, hi = -1e40;
+    for (int a = 0; a < w->natom; a++) {
+      double x = w->xyz[3 * a + j];
+      if (x - border < lo) lo = x - border;
+      if (x + border > hi) hi = x + border;
+    }
+    w->cell_lo[j] = lo;
+    w->aa[j] = hi - lo;
+    double b = border - fmax(2.0, 0.8 * border);
+    w->molborder[j] = fmax(b, 0.0) / (hi - lo);
+  }
+}
+
+owfn *o_wfn_new(int natom, const double *xyz, const int *z, int npri, int nmo,
+                const int *icenter, const int *itype, const double *e,
+                const double *occ, const double *cmo, int wfntyp, int nalpha) {
+  owfn *w = calloc(1, sizeof(owfn));
+  w->natom = natom;
+  w->xyz = malloc(sizeof(double) * 3 * natom);
+  memcpy(w->xyz, xyz, sizeof(double) * 3 * natom);
+  w->z = malloc(sizeof(int) * natom);
+  memcpy(w->z, z, sizeof(int) * natom);
+  w->npri = npri;
+  w->nmo = nmo;
+  w->icenter = malloc(sizeof(int) * npri);
+  w->itype = malloc(sizeof(int) * npri);
+  w->e = malloc(sizeof(double) * npri);
+  w->occ = malloc(sizeof(double) * nmo);
+  w->cmo = malloc(sizeof(double) * (size_t)npri * nmo);
+  for (int i = 0; i < npri; i++) {
+    w->icenter[i] = icenter[i] - 1;
+    w->itype[i] = itype[i];
+    w->e[i] = e[i];
+  }
+  memcpy(w->occ, occ, sizeof(double) * nmo);
+  memcpy(w->cmo, cmo, sizeof(double) * (size_t)npri * nmo);
+  w->wfntyp = wfntyp;
+  w->nalpha = nalpha;
+  prune_primitives(w);
+  complete_struct(w);
+  molecular_cell(w);
+  return w;
+}
+
+void o_wfn_free(owfn *w) {
+  if (!w) return;
+  free(w->xyz); free(w->z); free(w->icenter); free(w->itype); free(w->e);
+  free(w->occ); free(w->cmo); free(w->dran); free(w->spcutoff); free(w->lmax);
+  free(w->icord); free(w->iprilo); free(w->iprihi);
+  free(w);
+}
+
+int o_wfn_npri(const owfn *w) { return w->npri; }
+
+void o_wfn_cell(const owfn *w, double lo[3], double aa[3], double mb[3]) {
+  for (int j = 0; j < 3; j++) lo[j] = w->cell_lo[j], aa[j] = w->aa[j], mb[j] = w->molborder[j];
+}
+
+static double ipow(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; i++) r *= x;
+  return r;
+}
+
+/* calculate_mo_gto, src/wfn_private@proc.F90:3161-3273.  The environment is
+ * the set of atoms with d^2 <= spcutoff^2 (list_near_atoms with up2dcidx,
+ * src/crystalmod@env.f90:409-410; for a molecule the block walk returns the
+ * same set).  phi is (10, nmo): component-major, MO fastest. */
+static void calculate_mo_gto(const owfn *w, const double xpos[3], int nder, double *phi) {
+  static const int imax[3] = {1, 4, 10};
+  int nmo = w->nmo, nc = imax[nder];
+  memset(phi, 0, sizeof(double) * 10 * nmo);
+  for (int a = 0; a < w->natom; a++) {
+    double xx[3], dd = 0.0;
+    for (int j = 0; j < 3; j++) {
+      xx[j] = xpos[j] - w->xyz[3 * a + j];
+      dd += xx[j] * xx[j];
+    }
+    if (!(dd <= w->spcutoff[a] * w->spcutoff[a])) continue;
+    double dist = sqrt(dd);
+    double d2 = dist * dist;
+    double xl[3][3][6];
+    int lm = w->lmax[a];
+    for (int ix = 0; ix < 3; ix++) {
+      xl[ix][0][0] = 1.0; xl[ix][1][0] = 0.0; xl[ix][2][0] = 0.0;
+      if (lm < 1) continue;
+      xl[ix][0][1] = xx[ix]; xl[ix][1][1] = 1.0; xl[ix][2][1] = 0.0;
+      if (lm < 2) continue;
+      xl[ix][0][2] = xl[ix][0][1] * xx[ix]; xl[ix][1][2] = 2.0 * xl[ix][0][1]; xl[ix][2][2] = 2.0;
+      if (lm < 3) continue;
+      xl[ix][0][3] = xl[ix][0][2] * xx[ix]; xl[ix][1][3] = 3.0 * xl[ix][0][2]; xl[ix][2][3] = 6.0 * xl[ix][0][1];
+      if (lm < 4) continue;
+      xl[ix][0][4] = xl[ix][0][3] * xx[ix]; xl[ix][1][4] = 4.0 * xl[ix][0][3]; xl[ix][2][4] = 12.0 * xl[ix][0][2];
+      if (lm < 5) continue;
+      xl[ix][0][5] = xl[ix][0][4] * xx[ix]; xl[ix][1][5] = 5.0 * xl[ix][0][4]; xl[ix][2][5] = 20.0 * xl[ix][0][3];
+    }
+    for (int j = w->iprilo[a]; j <= w->iprihi[a]; j++) {
+      int ip = w->icord[j];
+      if (dist > w->dran[ip]) continue;
+      double al = w->e[ip];
+      double ex = exp(-al * d2);
+      const int *l = LI[w->itype[ip] - 1];
+      double chi[10];
+      chi[0] = xl[0][0][l[0]] * xl[1][0][l[1]] * xl[2][0][l[2]] * ex;
+      if (nder > 0) {
+        double f1x = xl[0][1][l[0]] - 2 * al * ipow(xx[0], l[0] + 1);
+        double f1y = xl[1][1][l[1]] - 2 * al * ipow(xx[1], l[1] + 1);
+        double f1z = xl[2][1][l[2]] - 2 * al * ipow(xx[2], l[2] + 1);
+        chi[1] = f1x * xl[1][0][l[1]] * xl[2][0][l[2]] * ex;
+        chi[2] = f1y * xl[0][0][l[0]] * xl[2][0][l[2]] * ex;
+        chi[3] = f1z * xl[0][0][l[0]] * xl[1][0][l[1]] * ex;
+        if (nder > 1) {
+          chi[4] = (xl[0][2][l[0]] - 2 * al * (2 * l[0] + 1) * xl[0][0][l[0]] + 4 * al * al * ipow(xx[0], l[0] + 2)) *
+                   xl[1][0][l[1]] * xl[2][0][l[2]] * ex;
+          chi[5] = (xl[1][2][l[1]] - 2 * al * (2 * l[1] + 1) * xl[1][0][l[1]] + 4 * al * al * ipow(xx[1], l[1] + 2)) *
+                   xl[2][0][l[2]] * xl[0][0][l[0]] * ex;
+          chi[6] = (xl[2][2][l[2]] - 2 * al * (2 * l[2] + 1) * xl[2][0][l[2]] + 4 * al * al * ipow(xx[2], l[2] + 2)) *
+                   xl[0][0][l[0]] * xl[1][0][l[1]] * ex;
+          chi[7] = f1x * f1y * xl[2][0][l[2]] * ex;
+          chi[8] = f1x * f1z * xl[1][0][l[1]] * ex;
+          chi[9] = f1z * f1y * xl[0][0][l[0]] * ex;
+        }
+      }
+      const double *c = w->cmo + (size_t)ip * nmo;
+      for (int ix = 0; ix < nc; ix++) {
+        double cx = chi[ix];
+        double *p = phi + (size_t)ix * nmo;
+        for (int m = 0; m < nmo; m++) p[m] += c[m] * cx;
+      }
+    }
+  }
+}
+
+/* molwfn%rho2, src/wfn_private@proc.F90:2484-2705 (no EDF core). Output
+ * arrays are Fortran-ordered: rho(3) = total/up/down, grad(3,3) column j =
+ * spin j, h(3,3,3) column-major per spin, stress(3,3). */
+void o_rho2(const owfn *w, const double xpos[3], int nder, double rho[3], double rhoval[3],
+            double grad[9], double gradval[9], double h[27], double hval[27],
+            double gkin[3], double *vir, double stress[9]) {
+  int nmo = w->nmo;
+  double *phi = malloc(sizeof(double) * 10 * nmo);
+  double hh[3][6] = {{0}}, hhval[3][6];
+  double g[3][3] = {{0}}, gk[3] = {0}, st[3][3] = {{0}}, rh[3] = {0};
+  calculate_mo_gto(w, xpos, nder, phi);
+  const double *p0 = phi, *px = phi + nmo, *py = phi + 2 * nmo, *pz = phi + 3 * nmo;
+  const double *pxx = phi + 4 * nmo, *pyy = phi + 5 * nmo, *pzz = phi + 6 * nmo;
+  const double *pxy = phi + 7 * nmo, *pxz = phi + 8 * nmo, *pyz = phi + 9 * nmo;
+  int uhf = (w->wfntyp == 1), rohf = (w->wfntyp == 2);
+  for (int m = 0; m < nmo; m++) {
+    double aocc = w->occ[m];
+    int isalpha = (m < w->nalpha);
+    double rs = aocc * p0[m] * p0[m];
+    rh[0] += rs;
+    if (uhf) rh[isalpha ? 1 : 2] += rs;
+    else if (rohf) { rh[1] += rs; if (isalpha) rh[2] += rs; }
+    if (nder > 0) {
+      double gs[3] = {2 * aocc * p0[m] * px[m], 2 * aocc * p0[m] * py[m], 2 * aocc * p0[m] * pz[m]};
+      double ks = aocc * (px[m] * px[m] + py[m] * py[m] + pz[m] * pz[m]);
+      for (int j = 0; j < 3; j++) g[0][j] += gs[j];
+      gk[0] += ks;
+      if (uhf) { int s = isalpha ? 1 : 2; for (int j = 0; j < 3; j++) g[s][j] += gs[j]; gk[s] += ks; }
+      else if (rohf) {
+        for (int j = 0; j < 3; j++) g[1][j] += gs[j];
+        gk[1] += ks;
+        if (isalpha) { for (int j = 0; j < 3; j++) g[2][j] += gs[j]; gk[2] += ks; }
+      }
+    }
+    if (nder > 1) {
+      double hs[6];
+      hs[0] = 2 * aocc * (p0[m] * pxx[m] + px[m] * px[m]);
+      hs[1] = 2 * aocc * (p0[m] * pyy[m] + py[m] * py[m]);
+      hs[2] = 2 * aocc * (p0[m] * pzz[m] + pz[m] * pz[m]);
+      hs[3] = 2 * aocc * (p0[m] * pxy[m] + px[m] * py[m]);
+      hs[4] = 2 * aocc * (p0[m] * pxz[m] + px[m] * pz[m]);
+      hs[5] = 2 * aocc * (p0[m] * pyz[m] + py[m] * pz[m]);
+      for (int j = 0; j < 6; j++) hh[0][j] += hs[j];
+      if (uhf) { int s = isalpha ? 1 : 2; for (int j = 0; j < 6; j++) hh[s][j] += hs[j]; }
+      else if (rohf) {
+        for (int j = 0; j < 6; j++) hh[1][j] += hs[j];
+        if (isalpha) for (int j = 0; j < 6; j++) hh[2][j] += hs[j];
+      }
+      st[0][0] += aocc * (p0[m] * pxx[m] - px[m] * px[m]);
+      st[0][1] += aocc * (p0[m] * pxy[m] - px[m] * py[m]);
+      st[0][2] += aocc * (p0[m] * pxz[m] - px[m] * pz[m]);
+      st[1][1] += aocc * (p0[m] * pyy[m] - py[m] * py[m]);
+      st[1][2] += aocc * (p0[m] * pyz[m] - py[m] * pz[m]);
+      st[2][2] += aocc * (p0[m] * pzz[m] - pz[m] * pz[m]);
+    }
+  }
+  free(phi);
+  /* core density contribution is zero (nedf = 0) */
+  if (!uhf && !rohf) {
+    rhoval[0] = rh[0]; rhoval[1] = 0.5 * rh[0]; rhoval[2] = rhoval[1];
+    rh[1] = 0.5 * rh[0]; rh[2] = rh[1];
+    for (int j = 0; j < 3; j++) {
+      gradval[j] = g[0][j]; gradval[3 + j] = 0.5 * g[0][j]; gradval[6 + j] = 0.5 * g[0][j];
+      g[1][j] = 0.5 * g[0][j]; g[2][j] = g[1][j];
+    }
+    gk[1] = gk[0] / 2; gk[2] = gk[1];
+    for (int j = 0; j < 6; j++) {
+      hhval[0][j] = hh[0][j]; hhval[1][j] = 0.5 * hh[0][j]; hhval[2][j] = hhval[1][j];
+      hh[1][j] = 0.5 * hh[0][j]; hh[2][j] = hh[1][j];
+    }
+  } else {
+    for (int s = 0; s < 3; s++) {
+      rhoval[s] = rh[s];
+      for (int j = 0; j < 3; j++) gradval[3 * s + j] = g[s][j];
+      for (int j = 0; j < 6; j++) hhval[s][j] = hh[s][j];
+    }
+  }
+  for (int s = 0; s < 3; s++) rho[s] = rh[s];
+  for (int s = 0; s < 3; s++)
+    for (int j = 0; j < 3; j++) grad[3 * s + j] = g[s][j];
+  st[1][0] = st[0][1]; st[2][0] = st[0][2]; st[2][1] = st[1][2];
+  double v = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) { st[i][j] *= 0.5; stress[3 * j + i] = st[i][j]; }
+  v = st[0][0] + st[1][1] + st[2][2];
+  *vir = v;
+  for (int s = 0; s < 3; s++) {
+    gkin[s] = 0.5 * gk[s];
+    double *H = h + 9 * s, *HV = hval + 9 * s;
+    /* column-major H(i,j) at 3*j+i */
+    H[0] = hh[s][0]; H[4] = hh[s][1]; H[8] = hh[s][2];
+    H[3] = H[1] = hh[s][3]; H[6] = H[2] = hh[s][4]; H[7] = H[5] = hh[s][5];
+    HV[0] = hhval[s][0]; HV[4] = hhval[s][1]; HV[8] = hhval[s][2];
+    HV[3] = HV[1] = hhval[s][3]; HV[6] = HV[2] = hhval[s][4]; HV[7] = HV[5] = hhval[s][5];
+  }
+}
+
+/* Symmetric 3x3 eigenvalues in ascending order (the role of LAPACK dsyev in
+ * eigsym, src/tools_math@proc.f90:1005-1039).  Cyclic Jacobi rotations. */
+void o_eigsym3(const double m[9], double ev[3]) {
+  double a[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) a[i][j] = 0.5 * (m[3 * j + i] + m[3 * i + j]);
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    double dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off == 0.0 || off < 1e-34 * dia) break;
+    for (int p = 0; p < 2; p++)
+      for (int q = p + 1; q < 3; q++) {
+        if (a[p][q] == 0.0) continue;
+        double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; k++) {
+          double akp = a[k][p], akq = a[k][q];
+          a[k][p] = c * akp - s * akq;
+          a[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; k++) {
+          double apk = a[p][k], aqk = a[q][k];
+          a[p][k] = c * apk - s * aqk;
+          a[q][k] = s * apk + c * aqk;
+        }
+      }
+  }
+  double e0 = a[0][0], e1 = a[1][1], e2 = a[2][2], t;
+  if (e0 > e1) t = e0, e0 = e1, e1 = t;
+  if (e1 > e2) t = e1, e1 = e2, e2 = t;
+  if (e0 > e1) t = e0, e0 = e1, e1 = t;
+  ev[0] = e0; ev[1] = e1; ev[2] = e2;
+}
+
+/* rsindex, src/tools_math@proc.f90:1084-1106: rank and signature with a
+ * zero threshold eps. */
+void o_rsindex(const double m[9], double ev[3], int *r, int *s, double eps) {
+  o_eigsym3(m, ev);
+  int np = 0, nm = 0;
+  for (int i = 0; i < 3; i++) {
+    if (ev[i] > eps) np++;
+    if (ev[i] < -eps) nm++;
+  }
+  *r = np + nm;
+  *s = np - nm;
+}
+
+/* matinvsym for n = 3 (src/tools_math@proc.f90:1276-1316): inverse of a
+ * symmetric matrix; nonzero return when the matrix is exactly singular
+ * (the LDL^T factor has a zero pivot). */
+int o_matinvsym3(double m[9]) {
+  double a = m[0], b = m[3], c = m[6], d = m[4], e = m[7], f = m[8];
+  double A = d * f - e * e, B = c * e - b * f, C = b * e - c * d;
+  double det = a * A + b * B + c * C;
+  if (det == 0.0 || !isfinite(det)) return 1;
+  double D = a * f - c * c, E = b * c - a * e, F = a * d - b * b;
+  double id = 1.0 / det;
+  m[0] = A * id; m[4] = D * id; m[8] = F * id;
+  m[1] = m[3] = B * id; m[2] = m[6] = C * id; m[5] = m[7] = E * id;
+  return 0;
+}
+
+/* nearest atom within distmax (identify_atom for a molecule,
+ * src/crystalmod@env.f90:593-614). Returns the 0-based atom or -1. */
+static int identify_atom(const owfn *w, const double x[3], double distmax, double *dist) {
+  int best = -1;
+  double dmin = 1e30;
+  for (int a = 0; a < w->natom; a++) {
+    double dx = x[0] - w->xyz[3 * a], dy = x[1] - w->xyz[3 * a + 1], dz = x[2] - w->xyz[3 * a + 2];
+    double d = sqrt(dx * dx + dy * dy + dz * dz);
+    if (d < dmin) dmin = d, best = a;
+  }
+  if (dist) *dist = dmin;
+  return (dmin <= distmax) ? best : -1;
+}
+
+/* field%grd for a molecular wavefunction, src/fieldmod@proc.f90:808-1171:
+ * wrap into the molecular cell (:921-943), rho2 (:1002-1047), nucleus
+ * check within 1e-5 bohr -> zero gradient (:1148-1154), rank/signature with
+ * CP_hdegen (:1157-1162). */
+void o_grd(const owfn *w, const double v[3], int nder, ores *res) {
+  memset(res, 0, sizeof(*res));
+  res->valid = 1;
+  double wc[3];
+  for (int j = 0; j < 3; j++) {
+    double x = (v[j] - w->cell_lo[j]) / w->aa[j];
+    if (x < -FLOOREPS || x > 1.0 + FLOOREPS) x -= floor(x);
+    wc[j] = w->cell_lo[j] + x * w->aa[j];
+  }
+  double rho[3], rhov[3], g[9], gv[9], h[27], hv[27], gk[3], vir, st[9];
+  o_rho2(w, wc, nder, rho, rhov, g, gv, h, hv, gk, &vir, st);
+  res->f = rho[0];
+  res->fval = rhov[0];
+  res->fspin[0] = rho[1];
+  res->fspin[1] = rho[2];
+  if (nder > 0) {
+    for (int j = 0; j < 3; j++) res->gf[j] = g[j];
+    res->gfmodval = sqrt(gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]);
+    res->gfmodspin[0] = sqrt(g[3] * g[3] + g[4] * g[4] + g[5] * g[5]);
+    res->gfmodspin[1] = sqrt(g[6] * g[6] + g[7] * g[7] + g[8] * g[8]);
+    res->gkin = gk[0];
+    res->gkinspin[0] = gk[1];
+    res->gkinspin[1] = gk[2];
+  }
+  if (nder > 1) {
+    memcpy(res->hf, h, sizeof(double) * 9);
+    res->del2fval = hv[0] + hv[4] + hv[8];
+    res->lapspin[0] = h[9] + h[13] + h[17];
+    res->lapspin[1] = h[18] + h[22] + h[26];
+    memcpy(res->stress, st, sizeof(st));
+    res->vir = vir;
+  }
+  res->isnuc = identify_atom(w, wc, 1e-5, NULL) >= 0;
+  if (nder > 0) {
+    if (res->isnuc) res->gf[0] = res->gf[1] = res->gf[2] = 0.0;
+    res->gfmod = sqrt(res->gf[0] * res->gf[0] + res->gf[1] * res->gf[1] + res->gf[2] * res->gf[2]);
+  }
+  if (nder > 1) {
+    res->del2f = res->hf[0] + res->hf[4] + res->hf[8];
+    o_rsindex(res->hf, res->hfeval, &res->r, &res->s, CP_HDEGEN);
+  }
+}
+
+/* NCI per-point body, src/nci@proc.f90:565-571 and 598-599:
+ * s = |grad rho| / (2 (3 pi^2)^(1/3) max(rho,vsmall)^(4/3)),
+ * crho = sign(rho, lambda2) * 100. */
+static void nci_point(const owfn *w, const double x[3], double *crho, double *cgrad) {
+  const double cst = 2.0 * pow(3.0 * M_PI * M_PI, 1.0 / 3.0);
+  ores res;
+  o_grd(w, x, 2, &res);
+  double ev[3];
+  o_eigsym3(res.hf, ev);
+  *cgrad = res.gfmod / (cst * pow(fmax(res.f, VSMALL), 4.0 / 3.0));
+  *crho = copysign(fabs(res.f), ev[1]) * 100.0;
+}
+
+void o_nci_points(const owfn *w, long n, const double *xyz, double *crho, double *cgrad,
+                  int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long i = 0; i < n; i++) nci_point(w, xyz + 3 * i, crho + i, cgrad + i);
+}
+
+/* The nciplot grid loop, src/nci@proc.f90:543-605: OpenMP dynamic over the
+ * outermost index i; arrays laid out (k, j, i) with k fastest; x = x0 +
+ * i*xmat(:,1) + j*xmat(:,2) + k*xmat(:,3).  Rows i0..i1-1 only (bounded
+ * samples); outputs are indexed from row i0. */
+void o_nciplot(const owfn *w, const double x0[3], const double xmat[9], const int nstep[3],
+               int i0, int i1, double *crho, double *cgrad, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  int n2 = nstep[1], n3 = nstep[2];
+#pragma omp parallel for schedule(dynamic)
+  for (int i = i0; i < i1; i++)
+    for (int j = 0; j < n2; j++)
+      for (int k = 0; k < n3; k++) {
+        double x[3];
+        for (int c = 0; c < 3; c++) x[c] = x0[c] + i * xmat[c] + j * xmat[3 + c] + k * xmat[6 + c];
+        size_t idx = ((size_t)(i - i0) * n2 + j) * n3 + k;
+        nci_point(w, x, crho + idx, cgrad + idx);
+      }
+}
+
+void o_rho2_points(const owfn *w, long n, const double *xyz, int nder, double *rho,
+                   double *grad, double *hess, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long i = 0; i < n; i++) {
+    double r[3], rv[3], g[9], gv[9], h[27], hv[27], gk[3], vir, st[9];
+    o_rho2(w, xyz + 3 * i, nder, r, rv, g, gv, h, hv, gk, &vir, st);
+    rho[i] = r[0];
+    if (grad) for (int j = 0; j < 3; j++) grad[3 * i + j] = g[j];
+    if (hess) for (int j = 0; j < 9; j++) hess[9 * i + j] = h[j];
+  }
+}
+
+/* field%newton, src/fieldmod@proc.f90:2238-2279: ier 0 converged,
+ * 1 invalid/singular Hessian, 2 too many iterations. */
+int o_newton(const owfn *w, double r[3], double gfnormeps, int maxit) {
+  for (int it = 0; it < maxit; it++) {
+    ores res;
+    o_grd(w, r, 2, &res);
+    if (!res.valid) return 1;
+    if (res.gfmod < gfnormeps) return 0;
+    if (o_matinvsym3(res.hf)) return 1;
+    double *H = res.hf;
+    double d0 = H[0] * res.gf[0] + H[3] * res.gf[1] + H[6] * res.gf[2];
+    double d1 = H[1] * res.gf[0] + H[4] * res.gf[1] + H[7] * res.gf[2];
+    double d2 = H[2] * res.gf[0] + H[5] * res.gf[1] + H[8] * res.gf[2];
+    r[0] -= d0; r[1] -= d1; r[2] -= d2;
+  }
+  return 2;
+}
+
+void o_newton_batch(const owfn *w, long n, double *xyz, double gfnormeps, int maxit,
+                    int *ier, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic)
+  for (long i = 0; i < n; i++) ier[i] = o_newton(w, xyz + 3 * i, gfnormeps, maxit);
+}
+
+/* Default molecular seeding, src/autocp@proc.f90:423-437 (pairs within
+ * maxdist, npts points at fractions k/(npts+1)), then the molecular-cell
+ * border filter (:672-693).  Returns the number of seeds written. */
+int o_pair_seeds(const owfn *w, double maxdist, int npts, double *xseed, int maxseed) {
+  int nn = 0;
+  for (int i1 = 0; i1 < w->natom; i1++)
+    for (int i2 = 0; i2 < w->natom; i2++) {
+      if (i1 == i2) continue;
+      const double *a = w->xyz + 3 * i1, *b = w->xyz + 3 * i2;
+      double d = sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) +
+                      (a[2] - b[2]) * (a[2] - b[2]));
+      if (d > maxdist) continue;
+      for (int k = 1; k <= npts; k++) {
+        double x[3], keep = 1;
+        for (int c = 0; c < 3; c++) {
+          double xa = (a[c] - w->cell_lo[c]) / w->aa[c], xb = (b[c] - w->cell_lo[c]) / w->aa[c];
+          double xf = xa + (double)k / (double)(npts + 1) * (xb - xa);
+          xf -= floor(xf);
+          if (xf < w->molborder[c] || xf > 1.0 - w->molborder[c]) keep = 0;
+          x[c] = w->cell_lo[c] + xf * w->aa[c];
+        }
+        if (!keep) continue;
+        if (nn < maxseed) memcpy(xseed + 3 * nn, x, sizeof(x));
+        nn++;
+      }
+    }
+  return nn;
+}
+
+typedef struct {
+  double x[3]; /* cell-fractional */
+  double r[3]; /* Cartesian */
+  double f;
+  int typ, typind, isnuc;
+} ocp;
+
+/* field%addcp for a molecule, src/fieldmod@proc.f90:2288-2439 (no
+ * symmetry: every CP has multiplicity 1). Returns 1 when the CP is added. */
+static int addcp(const owfn *w, const double x0[3], double cpeps, double nuceps,
+                 double nucepsh, double gfnormeps, ocp *cps, int *ncp, int maxcp) {
+  double xc[3], x1[3];
+  for (int j = 0; j < 3; j++) {
+    xc[j] = (x0[j] - w->cell_lo[j]) / w->aa[j];
+    xc[j] -= floor(xc[j]);
+    if (xc[j] < w->molborder[j] || xc[j] > 1.0 - w->molborder[j]) return 0;
+    x1[j] = w->cell_lo[j] + xc[j] * w->aa[j];
+  }
+  /* nearest CP (nearest_cp, src/fieldmod@proc.f90:1883-1933) */
+  int nid = -1;
+  double dmin = 1e30;
+  for (int i = 0; i < *ncp; i++) {
+    double t[3], dd = 0;
+    for (int j = 0; j < 3; j++) {
+      t[j] = (cps[i].x[j] - (xc[j] - floor(xc[j]))) * w->aa[j];
+      dd += t[j] * t[j];
+    }
+    dd = sqrt(dd);
+    if (dd < dmin) dmin = dd, nid = i;
+  }
+  if (nid >= w->natom && dmin < cpeps) return 0;
+  double dist;
+  int at = identify_atom(w, x1, fmax(nuceps, nucepsh), &dist);
+  if (at >= 0) {
+    if (w->z[at] == 1) { if (dist < nucepsh) return 0; }
+    else if (dist < nuceps) return 0;
+  }
+  ores res;
+  o_grd(w, x1, 2, &res);
+  if (!res.valid) return 0;
+  if (res.gfmod >= gfnormeps) return 0;
+  if (res.r != 3) return 0; /* degenerate CP discarded */
+  if (*ncp >= maxcp) return 0;
+  ocp *c = cps + (*ncp)++;
+  memcpy(c->x, xc, sizeof(xc));
+  memcpy(c->r, x1, sizeof(x1));
+  c->f = res.f;
+  c->typ = res.s;
+  c->typind = (res.s + 3) / 2;
+  c->isnuc = 0;
+  return 1;
+}
+
+/* autocritic core, src/autocp@proc.f90:755-822: Newton from every seed
+ * (parallel), addcp on the converged ones (serial, in seed order, which is
+ * one valid order of the reference's omp critical section), then sortcps
+ * (src/fieldmod@proc.f90:2441-2466): non-nuclear CPs by type, then by
+ * decreasing density.  Outputs Cartesian positions, types and densities;
+ * nuc_count[4] = n, b, r, c counts.  Returns ncp. */
+int o_autocritic(const owfn *w, int nseed, const double *xseed, int nthreads, int maxcp,
+                 double *cp_xyz, int *cp_typ, double *cp_f, int *nuc_count) {
+  const double gfnormeps = 1e-12, cpeps = 1e-2, nuceps = 1e-1, nucepsh = 2e-1;
+  double *x = malloc(sizeof(double) * 3 * (size_t)(nseed > 0 ? nseed : 1));
+  int *ier = malloc(sizeof(int) * (size_t)(nseed > 0 ? nseed : 1));
+  memcpy(x, xseed, sizeof(double) * 3 * (size_t)nseed);
+  o_newton_batch(w, nseed, x, gfnormeps, 200, ier, nthreads);
+  int cap = w->natom + nseed + 1;
+  ocp *cps = calloc((size_t)cap, sizeof(ocp));
+  int ncp = 0;
+  /* init_cplist: nuclei first (src/fieldmod@proc.f90:1795-1852) */
+  for (int a = 0; a < w->natom; a++) {
+    ocp *c = cps + ncp++;
+    for (int j = 0; j < 3; j++) {
+      c->r[j] = w->xyz[3 * a + j];
+      c->x[j] = (c->r[j] - w->cell_lo[j]) / w->aa[j];
+      c->x[j] -= floor(c->x[j]);
+    }
+    c->typ = -3; c->typind = 0; c->isnuc = 1;
+    ores res;
+    o_grd(w, c->r, 2, &res);
+    c->f = res.f;
+  }
+  for (int i = 0; i < nseed; i++)
+    if (ier[i] <= 0) addcp(w, x + 3 * i, cpeps, nuceps, nucepsh, fmax(1e-4, gfnormeps), cps, &ncp, cap);
+  /* sortcps: stable sort by -f, then stable sort by typind (non-nuclear part) */
+  int nn = ncp - w->natom;
+  ocp *tail = cps + w->natom;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int i = 1; i < nn; i++) {
+      ocp t = tail[i];
+      int j = i - 1;
+      while (j >= 0 && (pass == 0 ? (-tail[j].f > -t.f) : (tail[j].typind > t.typind))) {
+        tail[j + 1] = tail[j];
+        j--;
+      }
+      tail[j + 1] = t;
+    }
+  }
+  for (int k = 0; k < 4; k++) nuc_count[k] = 0;
+  for (int i = 0; i < ncp; i++) {
+    nuc_count[cps[i].typind]++;
+    if (i < maxcp) {
+      memcpy(cp_xyz + 3 * i, cps[i].r, sizeof(double) * 3);
+      cp_typ[i] = cps[i].typ;
+      cp_f[i] = cps[i].f;
+    }
+  }
+  free(x);
+  free(ier);
+  free(cps);
+  return ncp;
+}

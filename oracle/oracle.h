@@ -1,0 +1,82 @@
+/*
+ * CPU oracle for the critic2 molecular-wavefunction evaluator path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain C (+OpenMP) restatement of
+ * critic2's FP64 algorithm for the path (rho2 / calculate_mo_gto, field%grd,
+ * the NCI grid loop, field%newton, field%addcp, autocritic pair seeding and
+ * the Poincare-Hopf count).  It is the checker the GPU library's results are
+ * compared against, and the timed CPU baseline ("port") in bench.py.  The
+ * product library never links, loads or calls it.
+ *
+ * Parity status: the post-processing (3x3 eigen-solve, rank/signature, spin
+ * halves, Laplacian, |grad|, NCI reduced gradient) is pinned against the
+ * POINT records in critic2's own test references (tests/golden).  The GTO
+ * evaluator itself is pinned only by known-answer tests (analytic single
+ * primitives, finite differences, normalisation integrals): the reference
+ * cannot be compiled on these machines (no Fortran compiler) and its
+ * wavefunction test inputs are not distributed with the source.
+ *
+ * Conventions: Cartesian bohr; cmo is (npri, nmo) C order = Fortran
+ * cmo(nmo,npri); icenter/itype are 1-based on input.
+ */
+#ifndef CRITIC2_ORACLE_H
+#define CRITIC2_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct owfn owfn;
+
+/* scalar_value subset (src/types.f90:218-258) */
+typedef struct {
+  double f, fval;
+  double gf[3];
+  double gfmod, gfmodval;
+  double hf[9];          /* column-major 3x3 */
+  double hfeval[3];      /* ascending */
+  double del2f, del2fval;
+  double gkin;
+  double fspin[2], gkinspin[2], lapspin[2], gfmodspin[2];
+  double stress[9];
+  double vir;
+  int r, s, isnuc, valid;
+} ores;
+
+owfn *o_wfn_new(int natom, const double *xyz, const int *z, int npri, int nmo,
+                const int *icenter, const int *itype, const double *e,
+                const double *occ, const double *cmo, int wfntyp, int nalpha);
+void o_wfn_free(owfn *w);
+int o_wfn_npri(const owfn *w);
+void o_wfn_cell(const owfn *w, double lo[3], double aa[3], double molborder[3]);
+
+void o_rho2(const owfn *w, const double xpos[3], int nder, double rho[3], double rhoval[3],
+            double grad[9], double gradval[9], double h[27], double hval[27],
+            double gkin[3], double *vir, double stress[9]);
+void o_grd(const owfn *w, const double v[3], int nder, ores *res);
+
+void o_eigsym3(const double m[9], double ev[3]);
+void o_rsindex(const double m[9], double ev[3], int *r, int *s, double eps);
+int o_matinvsym3(double m[9]);
+
+void o_nci_points(const owfn *w, long n, const double *xyz, double *crho, double *cgrad,
+                  int nthreads);
+void o_nciplot(const owfn *w, const double x0[3], const double xmat[9], const int nstep[3],
+               int i0, int i1, double *crho, double *cgrad, int nthreads);
+void o_rho2_points(const owfn *w, long n, const double *xyz, int nder, double *rho,
+                   double *grad, double *hess, int nthreads);
+
+int o_newton(const owfn *w, double r[3], double gfnormeps, int maxit);
+void o_newton_batch(const owfn *w, long n, double *xyz, double gfnormeps, int maxit,
+                    int *ier, int nthreads);
+
+/* autocritic with default molecular pair seeding.  Outputs the CP list in
+ * critic2's final order (nuclei first, then sortcps order).  Returns ncp. */
+int o_pair_seeds(const owfn *w, double maxdist, int npts, double *xseed, int maxseed);
+int o_autocritic(const owfn *w, int nseed, const double *xseed, int nthreads, int maxcp,
+                 double *cp_xyz, int *cp_typ, double *cp_f, int *nuc_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

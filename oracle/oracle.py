@@ -1,0 +1,193 @@
+"""ctypes wrapper of the C oracle (oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker, and by bench.py's CPU-baseline leg.  The product library
+(critic2_gb300) never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "liboracle.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    """Compiles oracle.c into oracle/_build/liboracle.so (gcc, OpenMP)."""
+    src = os.path.join(_HERE, "oracle.c")
+    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(_SO), exist_ok=True)
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-Wall",
+                               src, "-o", _SO, "-lm"])
+    return _SO
+
+
+class ORes(C.Structure):
+    _fields_ = [("f", C.c_double), ("fval", C.c_double), ("gf", C.c_double * 3),
+                ("gfmod", C.c_double), ("gfmodval", C.c_double), ("hf", C.c_double * 9),
+                ("hfeval", C.c_double * 3), ("del2f", C.c_double), ("del2fval", C.c_double),
+                ("gkin", C.c_double), ("fspin", C.c_double * 2), ("gkinspin", C.c_double * 2),
+                ("lapspin", C.c_double * 2), ("gfmodspin", C.c_double * 2),
+                ("stress", C.c_double * 9), ("vir", C.c_double), ("r", C.c_int),
+                ("s", C.c_int), ("isnuc", C.c_int), ("valid", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        L = _lib
+        L.o_wfn_new.restype = C.c_void_p
+        L.o_wfn_new.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp,
+                                C.c_int, C.c_int]
+        L.o_wfn_free.argtypes = [C.c_void_p]
+        L.o_wfn_npri.argtypes = [C.c_void_p]
+        L.o_wfn_cell.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.o_rho2.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                             C.POINTER(C.c_double), _dp]
+        L.o_grd.argtypes = [C.c_void_p, _dp, C.c_int, C.POINTER(ORes)]
+        L.o_eigsym3.argtypes = [_dp, _dp]
+        L.o_rsindex.argtypes = [_dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_double]
+        L.o_matinvsym3.argtypes = [_dp]
+        L.o_matinvsym3.restype = C.c_int
+        L.o_nci_points.argtypes = [C.c_void_p, C.c_long, _dp, _dp, _dp, C.c_int]
+        L.o_nciplot.argtypes = [C.c_void_p, _dp, _dp, _ip, C.c_int, C.c_int, _dp, _dp, C.c_int]
+        L.o_rho2_points.argtypes = [C.c_void_p, C.c_long, _dp, C.c_int, _dp, C.c_void_p,
+                                    C.c_void_p, C.c_int]
+        L.o_newton.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int]
+        L.o_newton.restype = C.c_int
+        L.o_newton_batch.argtypes = [C.c_void_p, C.c_long, _dp, C.c_double, C.c_int, _ip, C.c_int]
+        L.o_pair_seeds.argtypes = [C.c_void_p, C.c_double, C.c_int, _dp, C.c_int]
+        L.o_pair_seeds.restype = C.c_int
+        L.o_autocritic.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, C.c_int, _dp, _ip, _dp, _ip]
+        L.o_autocritic.restype = C.c_int
+    return _lib
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Wfn:
+    """Oracle wavefunction (prune_primitives + complete_struct applied)."""
+
+    def __init__(self, mol):
+        L = lib()
+        self.mol = mol
+        self.h = L.o_wfn_new(mol.natom, _f64(mol.atom_xyz.reshape(-1)), _i32(mol.atom_z),
+                             mol.npri, mol.nmo, _i32(mol.icenter), _i32(mol.itype), _f64(mol.e),
+                             _f64(mol.occ), _f64(mol.cmo.reshape(-1)), int(mol.wfntyp),
+                             int(mol.nalpha))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().o_wfn_free(self.h)
+            self.h = None
+
+    @property
+    def npri(self):
+        return lib().o_wfn_npri(self.h)
+
+    def cell(self):
+        lo, aa, mb = np.zeros(3), np.zeros(3), np.zeros(3)
+        lib().o_wfn_cell(self.h, lo, aa, mb)
+        return lo, aa, mb
+
+    def rho2(self, x, nder=2):
+        rho, rv, gv = np.zeros(3), np.zeros(3), np.zeros(9)
+        g, h, hv, gk, st = np.zeros(9), np.zeros(27), np.zeros(27), np.zeros(3), np.zeros(9)
+        vir = C.c_double()
+        lib().o_rho2(self.h, _f64(x), nder, rho, rv, g, gv, h, hv, gk, C.byref(vir), st)
+        return dict(rho=rho, rhoval=rv, grad=g.reshape(3, 3), gradval=gv.reshape(3, 3),
+                    h=h.reshape(3, 3, 3), hval=hv.reshape(3, 3, 3), gkin=gk, vir=vir.value,
+                    stress=st.reshape(3, 3))
+
+    def grd(self, x, nder=2):
+        r = ORes()
+        lib().o_grd(self.h, _f64(x), nder, C.byref(r))
+        return r
+
+    def rho2_points(self, xyz, nder=2, nthreads=0):
+        xyz = _f64(xyz).reshape(-1, 3)
+        n = xyz.shape[0]
+        rho = np.zeros(n)
+        grad = np.zeros((n, 3)) if nder > 0 else None
+        hess = np.zeros((n, 9)) if nder > 1 else None
+        lib().o_rho2_points(self.h, n, xyz.reshape(-1), nder, rho,
+                            grad.ctypes.data if grad is not None else None,
+                            hess.ctypes.data if hess is not None else None, nthreads)
+        return rho, grad, hess
+
+    def nci_points(self, xyz, nthreads=0):
+        xyz = _f64(xyz).reshape(-1, 3)
+        n = xyz.shape[0]
+        crho, cgrad = np.zeros(n), np.zeros(n)
+        lib().o_nci_points(self.h, n, xyz.reshape(-1), crho, cgrad, nthreads)
+        return crho, cgrad
+
+    def nciplot(self, x0, xmat, nstep, i0=0, i1=None, nthreads=0):
+        nstep = _i32(nstep)
+        i1 = int(nstep[0]) if i1 is None else i1
+        n = (i1 - i0) * int(nstep[1]) * int(nstep[2])
+        crho, cgrad = np.zeros(n), np.zeros(n)
+        xm = _f64(np.asarray(xmat).T.reshape(-1))  # column-major xmat(:,i)
+        lib().o_nciplot(self.h, _f64(x0), xm, nstep, i0, i1, crho, cgrad, nthreads)
+        shp = (i1 - i0, int(nstep[1]), int(nstep[2]))
+        return crho.reshape(shp), cgrad.reshape(shp)
+
+    def newton_batch(self, xyz, gfnormeps=1e-12, maxit=200, nthreads=0):
+        x = _f64(xyz).reshape(-1, 3).copy()
+        ier = np.zeros(x.shape[0], np.int32)
+        lib().o_newton_batch(self.h, x.shape[0], x.reshape(-1), gfnormeps, maxit, ier, nthreads)
+        return x, ier
+
+    def pair_seeds(self, maxdist=15.0, npts=5):
+        n = lib().o_pair_seeds(self.h, maxdist, npts, np.zeros(3), 0)
+        buf = np.zeros(3 * max(n, 1))
+        lib().o_pair_seeds(self.h, maxdist, npts, buf, n)
+        return buf[: 3 * n].reshape(n, 3)
+
+    def autocritic(self, seeds=None, nthreads=0):
+        if seeds is None:
+            seeds = self.pair_seeds()
+        seeds = _f64(seeds).reshape(-1, 3)
+        maxcp = self.mol.natom + seeds.shape[0] + 1
+        xyz, typ, f = np.zeros(3 * maxcp), np.zeros(maxcp, np.int32), np.zeros(maxcp)
+        cnt = np.zeros(4, np.int32)
+        ncp = lib().o_autocritic(self.h, seeds.shape[0], seeds.reshape(-1), nthreads, maxcp,
+                                 xyz, typ, f, cnt)
+        return dict(xyz=xyz[: 3 * ncp].reshape(ncp, 3), typ=typ[:ncp], f=f[:ncp],
+                    counts=cnt, ph=int(cnt[0] - cnt[1] + cnt[2] - cnt[3]))
+
+
+def eigsym3(m):
+    ev = np.zeros(3)
+    lib().o_eigsym3(_f64(np.asarray(m).T.reshape(-1)), ev)
+    return ev
+
+
+def rsindex(m, eps=1e-8):
+    ev = np.zeros(3)
+    r, s = C.c_int(), C.c_int()
+    lib().o_rsindex(_f64(np.asarray(m).T.reshape(-1)), ev, C.byref(r), C.byref(s), eps)
+    return ev, r.value, s.value
+
+
+def matinvsym3(m):
+    a = _f64(np.asarray(m).T.reshape(-1)).copy()
+    ier = lib().o_matinvsym3(a)
+    return a.reshape(3, 3).T, ier

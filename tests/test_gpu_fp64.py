@@ -1,0 +1,178 @@
+"""FP64 plain-form parity: the CUDA evaluator through the C ABI against the
+oracle, on seeded synthetic wavefunctions.  Bar: 1e-10 relative."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from critic2_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def mol12():
+    return synth.make_molecule("nci12")
+
+
+@pytest.fixture(scope="module")
+def pair12(gpu_lib, oracle_mod, mol12):
+    from critic2_gb300.wfn import Wavefunction
+    return Wavefunction(mol12), oracle_mod.Wfn(mol12)
+
+
+def variant(mol, wfntyp):
+    """The same primitives as an open-shell wavefunction."""
+    m = synth.Molecule(**{k: getattr(mol, k) for k in
+                          ("atom_xyz", "atom_z", "icenter", "itype", "e", "occ", "cmo")},
+                       wfntyp=wfntyp, nalpha=mol.nmo // 2 + 1, name=mol.name)
+    m.occ = m.occ.copy()
+    if wfntyp == 1:
+        m.occ[:] = 1.0
+    elif wfntyp == 2:
+        m.occ[m.nalpha:] = 1.0
+    return m
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+
+
+def close(a, b, rel=REL, scale=None):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    s = np.abs(b).max() if scale is None else scale
+    return np.all(np.abs(a - b) <= rel * np.maximum(np.abs(b), 1e-6 * s))
+
+
+def test_rho2_all_outputs(pair12, mol12):
+    g, o = pair12
+    rng = np.random.default_rng(0)
+    lo, hi = mol12.atom_xyz.min(0) - 2, mol12.atom_xyz.max(0) + 2
+    pts = rng.uniform(lo, hi, size=(300, 3))
+    for nder in (0, 1, 2):
+        out = g.rho2(pts, nder=nder, prec="fp64")
+        for i in range(0, 300, 7):
+            ref = o.rho2(pts[i], nder)
+            assert close(out["rho"][i], ref["rho"])
+            if nder > 0:
+                assert close(out["grad"][i], ref["grad"])
+                assert close(out["gkin"][i], ref["gkin"])
+            if nder > 1:
+                assert close(out["hess"][i], ref["h"])
+                assert close(out["stress"][i], ref["stress"], scale=np.abs(ref["h"]).max())
+                assert abs(out["vir"][i] - ref["vir"]) <= REL * max(1.0, np.abs(ref["stress"]).max())
+
+
+@pytest.mark.parametrize("wfntyp", [1, 2])
+def test_rho2_open_shell(gpu_lib, oracle_mod, mol12, wfntyp):
+    from critic2_gb300.wfn import Wavefunction
+    m = variant(mol12, wfntyp)
+    g, o = Wavefunction(m), oracle_mod.Wfn(m)
+    rng = np.random.default_rng(wfntyp)
+    pts = rng.uniform(mol12.atom_xyz.min(0), mol12.atom_xyz.max(0), size=(64, 3))
+    out = g.rho2(pts, 2, "fp64")
+    for i in range(64):
+        ref = o.rho2(pts[i], 2)
+        assert close(out["rho"][i], ref["rho"])
+        assert close(out["grad"][i], ref["grad"])
+        assert close(out["hess"][i], ref["h"])
+        assert close(out["gkin"][i], ref["gkin"])
+
+
+def test_grd(pair12, mol12):
+    g, o = pair12
+    rng = np.random.default_rng(3)
+    pts = np.concatenate([rng.uniform(mol12.atom_xyz.min(0), mol12.atom_xyz.max(0), size=(50, 3)),
+                          mol12.atom_xyz[:3] + 1e-7,          # on nuclei
+                          mol12.atom_xyz.max(0) + 40.0 * np.ones((1, 3))])  # wraps in the cell
+    out = g.grd(pts, 2, "fp64")
+    for i, p in enumerate(pts):
+        ref = o.grd(p, 2)
+        assert out["isnuc"][i] == ref.isnuc
+        assert close(out["f"][i], ref.f)
+        assert abs(out["gfmod"][i] - ref.gfmod) <= REL * max(abs(ref.gfmod), 1e-6 * abs(ref.f))
+        ev = np.array(ref.hfeval[:])
+        assert np.all(np.abs(out["hfeval"][i] - ev) <= REL * np.abs(ev).max())
+        assert (out["r"][i], out["s"][i]) == (ref.r, ref.s)
+
+
+def test_nciplot_small_grid(pair12, mol12):
+    g, o = pair12
+    x0, xm, ns = synth.nci_grid(mol12, 80, 0.1)
+    crho, cgrad, st = g.nciplot(x0, xm, ns, "fp64")
+    rr, rg = o.nciplot(x0, xm, ns)
+    assert crho.shape == rr.shape == (80, 80, 80)
+    assert rel_err(np.abs(crho), np.abs(rr)) < REL
+    assert rel_err(cgrad, rg) < REL
+    flips = np.sign(crho) != np.sign(rr)
+    # a sign may differ only where lambda2 is zero to rounding
+    if flips.any():
+        pts = synth.grid_points(x0, xm, ns).reshape(-1, 3)[flips.reshape(-1)]
+        for p in pts[:20]:
+            r = o.grd(p, 2)
+            ev = np.array(r.hfeval[:])
+            assert abs(ev[1]) < 1e-9 * np.abs(ev).max()
+    assert flips.mean() < 1e-4
+
+
+def test_nciplot_planes_nci60(gpu_lib, oracle_mod):
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("nci60")
+    g, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    x0, xm, ns = synth.nci_grid(mol, 200, 0.1)
+    for i in (0, 113):
+        x0i = x0 + i * xm[:, 0]
+        nsi = np.array([1, 200, 200], np.int32)
+        crho, cgrad, _ = g.nciplot(x0i, xm, nsi, "fp64")
+        rr, rg = o.nciplot(x0i, xm, nsi)
+        assert rel_err(np.abs(crho), np.abs(rr)) < REL
+        assert rel_err(cgrad, rg) < REL
+
+
+def test_wfx_roundtrip(gpu_lib, pair12, mol12):
+    from critic2_gb300.wfn import Wavefunction
+    g, _ = pair12
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "m.wfx")
+        synth.write_wfx(mol12, path)
+        gw = Wavefunction.from_wfx(path)
+    assert (gw.natom, gw.npri, gw.nmo) == (g.natom, g.npri, g.nmo)
+    pts = np.random.default_rng(4).uniform(2, 10, size=(40, 3))
+    a, b = g.rho2(pts, 2), gw.rho2(pts, 2)
+    assert close(a["hess"], b["hess"], rel=1e-13)
+
+
+def test_newton(pair12, mol12):
+    g, o = pair12
+    seeds = g.pair_seeds()
+    ref_seeds = o.pair_seeds()
+    assert np.array_equal(seeds, ref_seeds)
+    sub = seeds[::11]
+    xg, ierg = g.newton(sub, 1e-12, 200, "fp64")
+    xo, iero = o.newton_batch(sub, 1e-12, 200)
+    assert np.array_equal(ierg, iero)
+    ok = iero == 0
+    assert np.allclose(xg[ok], xo[ok], rtol=0, atol=1e-8)
+
+
+def test_autocritic(pair12):
+    g, o = pair12
+    res = g.autocritic(prec="fp64")
+    ref = o.autocritic()
+    assert list(res["counts"]) == list(ref["counts"])
+    assert res["ph"] == ref["ph"]
+    assert np.array_equal(res["typ"], ref["typ"])
+    assert np.allclose(res["xyz"], ref["xyz"], atol=1e-6)
+
+
+def test_error_paths(pair12, gpu_lib):
+    g, _ = pair12
+    with pytest.raises(gpu_lib.C2GError) as e:
+        g.rho2(np.zeros((2, 3)), nder=3)
+    assert e.value.code == 1
+    with pytest.raises(gpu_lib.C2GError):
+        g.nciplot(np.zeros(3), np.eye(3), [0, 4, 4])
