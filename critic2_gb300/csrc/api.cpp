@@ -134,11 +134,35 @@ std::vector<double> eval_records_fp64(Handle &h, int n, const double *xyz, int n
 std::vector<double> eval_records(Handle &h, int n, const double *xyz, int nder, int prec, bool full) {
   if (prec == C2G_PREC_FP64) return eval_records_fp64(h, n, xyz, nder, full);
   const int nr = kRecNci;
+  // The split kernel evaluates 32 points per tile relative to the tile's
+  // centroid; ordering the batch along a Morton curve keeps tiles compact.
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) lo[c] = std::min(lo[c], xyz[3 * i + c]), hi[c] = std::max(hi[c], xyz[3 * i + c]);
+  std::vector<uint64_t> key(n);
+  for (int i = 0; i < n; i++) {
+    uint64_t q[3], k = 0;
+    for (int c = 0; c < 3; c++) {
+      const double sp = hi[c] - lo[c];
+      q[c] = (uint64_t)(sp > 0 ? std::min(2097151.0, (xyz[3 * i + c] - lo[c]) / sp * 2097151.0) : 0.0);
+    }
+    for (int b = 0; b < 21; b++)
+      for (int c = 0; c < 3; c++) k |= ((q[c] >> b) & 1ull) << (3 * b + c);
+    key[i] = k;
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return key[a] < key[b]; });
+  std::vector<double> sorted(3 * (size_t)n);
+  for (int i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) sorted[3 * (size_t)i + c] = xyz[3 * (size_t)ord[i] + c];
   DevBuf dx(sizeof(double) * 3 * (size_t)n), dr(sizeof(double) * nr * (size_t)n);
-  C2G_CUDA(cudaMemcpy(dx.p, xyz, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice));
+  C2G_CUDA(cudaMemcpy(dx.p, sorted.data(), sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice));
   tc_points(h, prec, n, dx.as<double>(), dr.as<double>(), 0);
-  std::vector<double> rec((size_t)nr * n);
-  C2G_CUDA(cudaMemcpy(rec.data(), dr.p, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost));
+  std::vector<double> srec((size_t)nr * n), rec((size_t)nr * n);
+  C2G_CUDA(cudaMemcpy(srec.data(), dr.p, sizeof(double) * srec.size(), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; i++)
+    std::copy(srec.begin() + (size_t)i * nr, srec.begin() + (size_t)(i + 1) * nr, rec.begin() + (size_t)ord[i] * nr);
   if (full) {
     std::vector<double> out((size_t)kRecFull * n, 0.0);
     for (int i = 0; i < n; i++)
@@ -335,6 +359,18 @@ int c2g_wfn_destroy(c2g_wfn *hp) {
   });
 }
 
+int c2g_wfn_set_param(c2g_wfn *hp, int param, double value) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    if (param == C2G_PARAM_RECHECK_REL) {
+      require(value >= 0.0 && value < 1.0, "re-check threshold must be in [0, 1)");
+      tc_set_recheck(*h, value);
+    } else {
+      fail(C2G_ERR_ARG, "unknown parameter");
+    }
+  });
+}
+
 int c2g_wfn_info(const c2g_wfn *hp, int *natom, int *npri, int *nmo, int *wfntyp, int *nalpha) {
   return guarded([&] {
     require(hp != nullptr, "null handle");
@@ -437,11 +473,12 @@ int c2g_nciplot_dev(c2g_wfn *hp, const double *x0, const double *xmat, const int
       C2G_CUDA(cudaEventRecord(e0, st));
     }
     long nrecheck = 0;
+    double stage_frac = 1.0;
     if (prec == C2G_PREC_FP64) {
       launch_fp64_nci_grid(h->dev, gs, d_crho, d_cgrad, st);
       if (stats) C2G_CUDA(cudaEventRecord(e1, st));
     } else {
-      nrecheck = tc_nci_grid(*h, prec, gs, d_crho, d_cgrad, st, stats ? e1 : nullptr);
+      nrecheck = tc_nci_grid(*h, prec, gs, d_crho, d_cgrad, st, stats ? e1 : nullptr, &stage_frac);
     }
     if (stats) {
       C2G_CUDA(cudaEventRecord(e2, st));
@@ -453,6 +490,7 @@ int c2g_nciplot_dev(c2g_wfn *hp, const double *x0, const double *xmat, const int
       stats->nrecheck = nrecheck;
       stats->ms_kernel = a;
       stats->ms_recheck = b;
+      stats->stage_frac = stage_frac;
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       cudaEventDestroy(e2);

@@ -20,11 +20,12 @@
 #include <cuda_runtime.h>
 
 #include "c2g_internal.h"
+#include "points.cuh"
 
 namespace c2g {
 namespace {
 
-constexpr int TP = 32;     // points per tile
+constexpr int TP = kTilePoints;  // points per tile
 constexpr int NG = 8;      // MO groups = warps
 constexpr int KCH = 8;     // primitives per chunk (one per warp)
 constexpr int NTHR = TP * NG;
@@ -69,96 +70,6 @@ __device__ __forceinline__ void chi_eval(double dx, double dy, double dz, double
     chi[9] = fz1 * fy1 * fx0 * ex;
   }
 }
-
-// wrap a point into the molecular cell like field%grd does for molecules
-// (src/fieldmod@proc.f90:921-943; flooreps = 1e-4)
-__device__ __forceinline__ void wrap_cell(const DevWfn &w, double (&x)[3]) {
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    double f = (x[j] - w.cell_lo[j]) / w.cell_aa[j];
-    if (f < -1e-4 || f > 1.0 + 1e-4) {
-      f -= floor(f);
-      x[j] = w.cell_lo[j] + f * w.cell_aa[j];
-    }
-  }
-}
-
-// ------------------------------------------------------------ point sources
-struct ListSrc {
-  const double *xyz;
-  int n;
-  __device__ bool point(const DevWfn &w, int tile, int p, double (&x)[3], long &idx) const {
-    const long i = (long)tile * TP + p;
-    idx = i;
-    if (i >= n) return false;
-    x[0] = xyz[3 * i];
-    x[1] = xyz[3 * i + 1];
-    x[2] = xyz[3 * i + 2];
-    wrap_cell(w, x);
-    return true;
-  }
-};
-
-__device__ __forceinline__ void grid_xyz(const GridSpec &g, int i, int j, int k, double (&x)[3]) {
-#pragma unroll
-  for (int c = 0; c < 3; c++) x[c] = g.x0[c] + i * g.xmat[c] + j * g.xmat[3 + c] + k * g.xmat[6 + c];
-}
-
-// tiles of 4 (j) x 8 (k) points on one i plane
-struct GridSrc {
-  GridSpec g;
-  int ntj, ntk;
-  __device__ bool point(const DevWfn &w, int tile, int p, double (&x)[3], long &idx) const {
-    const int i = tile / (ntj * ntk);
-    const int r = tile - i * ntj * ntk;
-    const int j = (r / ntk) * 4 + (p >> 3);
-    const int k = (r % ntk) * 8 + (p & 7);
-    idx = -1;
-    if (j >= g.nstep[1] || k >= g.nstep[2]) return false;
-    idx = ((long)i * g.nstep[1] + j) * g.nstep[2] + k;
-    grid_xyz(g, i, j, k, x);
-    wrap_cell(w, x);
-    return true;
-  }
-};
-
-// a device list of linear grid indices (k fastest); count read on device
-struct GridListSrc {
-  GridSpec g;
-  const int *list;
-  const int *count;
-  __device__ bool point(const DevWfn &w, int tile, int p, double (&x)[3], long &idx) const {
-    const long t = (long)tile * TP + p;
-    idx = -1;
-    if (t >= *count) return false;
-    const long li = list[t];
-    const int k = (int)(li % g.nstep[2]);
-    const int j = (int)((li / g.nstep[2]) % g.nstep[1]);
-    const int i = (int)(li / ((long)g.nstep[2] * g.nstep[1]));
-    idx = li;
-    grid_xyz(g, i, j, k, x);
-    wrap_cell(w, x);
-    return true;
-  }
-};
-
-// points x(3, idx[t]) for t < *count (the live seeds of a Newton batch)
-struct IndexSrc {
-  const double *x;
-  const int *idx;
-  const int *count;
-  __device__ bool point(const DevWfn &w, int tile, int p, double (&xx)[3], long &out) const {
-    const long t = (long)tile * TP + p;
-    out = t;
-    if (t >= *count) return false;
-    const long i = idx[t];
-    xx[0] = x[3 * i];
-    xx[1] = x[3 * i + 1];
-    xx[2] = x[3 * i + 2];
-    wrap_cell(w, xx);
-    return true;
-  }
-};
 
 // ------------------------------------------------------------------ sinks
 struct RecSink {
@@ -305,6 +216,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_eval_fp64(DevWfn w, Src src, Sink s
   static_assert(NG * 8 * TP <= KCH * 10 * TP, "reduction buffer");
 
   const int tid = threadIdx.x, p = tid & 31, g = tid >> 5;
+  ntiles = src.tiles(ntiles);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     if (tid < TP) {
       double x[3] = {0.0, 0.0, 0.0};
@@ -317,7 +229,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_eval_fp64(DevWfn w, Src src, Sink s
       s_idx[tid] = idx;
     }
     for (int q = tid; q < NR * TP; q += NTHR) s_acc[q] = 0.0;
-    __syncthreads();
+    if (!__syncthreads_or(tid < TP && s_valid[tid])) continue;
     const double px = s_x[0][p], py = s_x[1][p], pz = s_x[2][p];
     const bool pvalid = s_valid[p];
 

@@ -149,6 +149,7 @@ void newton_batch_dev(Handle &h, int n, double *d_x, int *d_ier, double gfnormep
       hsp = hc[2 + nxt];
       cur = nxt;
     }
+    if (split) tc_check_error(h);
   } catch (...) {
     cudaFree(buf);
     cudaFree(rec);

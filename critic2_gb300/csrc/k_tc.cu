@@ -1,26 +1,1143 @@
-// Split-precision evaluator (placeholder until the tcgen05 kernel lands).
+// Split-precision GTO evaluator on the 5th-generation tensor cores.
+//
+// critic2's hot loop (src/wfn_private@proc.F90:3263-3268) is the product
+//   phi_c(mo, p) = sum_k cmo(mo, k) * chi_c(k, p),  c = value, 3 first and
+//   6 second derivatives,
+// followed by the MO reduction of rho2 (src/wfn_private@proc.F90:2546-2624).
+// Here it runs as 10 tcgen05 MMAs per K-step with
+//   M = 128 MOs (A = the coefficient tile, resident in tensor memory),
+//   N = 32 points (B = the basis block chi, built in shared memory),
+//   K = one 32-byte row of primitives (16 bf16 or 8 tf32),
+// in a 3-product split: A_hi*B_hi + A_hi*B_lo + A_lo*B_hi, FP32 accumulate.
+// The accumulators (10 x 32 columns for the hi*hi products, 4 x 32 for the
+// cross products of the value and gradient) and 4 coefficient stages (16
+// columns each) fill the SM's 512 TMEM columns.
+//
+// CTA roles (persistent, one CTA per SM, 12 warps):
+//   warps 0-3  load the coefficient stage (L2 -> registers -> tcgen05.st into
+//              TMEM) and run the epilogue: tcgen05.ld of phi, the
+//              occupation-weighted products, the MO reduction (cross-lane via
+//              shared memory), FP64 accumulation over MO tiles, and the NCI
+//              or record output;
+//   warp 4     allocates TMEM; lane 0 issues the MMAs and commits;
+//   warp 5     prepares each point tile: coordinates, per-atom offsets and
+//              the list of K-stages that any point of the tile can see (a
+//              stage is skipped only when every (point, primitive) pair in it
+//              is beyond critic2's cutoff, so skipping changes no result),
+//              ordered from the least to the most important one;
+//   warps 6-11 build the basis block chi (value, gradient, Hessian of every
+//              primitive at the 32 points, split hi/lo) for one K-stage each.
+// Hand-offs use mbarriers; tcgen05.commit releases shared stages and
+// signals the accumulators.  Every wait is bounded: on a timeout the CTA sets
+// an error flag, stops, drains its MMAs and frees TMEM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
 #include "k_tc.h"
+#include "points.cuh"
+#include "ptx_sm100.h"
 
 namespace c2g {
 
-struct TcOperands {
-  int dummy;
+struct __align__(16) PrimTC {
+  float al2e;      // alpha * log2(e)
+  float alpha;     // alpha, rounded to FP32 ...
+  float alpha_lo;  // ... and the remainder alpha - alpha_hi
+  float dran;      // cutoff distance (0 for padding)
+  int meta;        // atom << 12 | lx | ly << 4 | lz << 8
+  int pad[3];
 };
 
-TcOperands *tc_create(Handle &) { return new TcOperands{0}; }
-void tc_destroy(TcOperands *t) { delete t; }
+struct TcKind {
+  bool built = false;
+  int kps = 0;        // primitives per K-stage
+  int nstage = 0;
+  int kpad = 0;
+  PrimTC *prim = nullptr;
+  uint8_t *c_hi = nullptr, *c_lo = nullptr;  // [mo_pad][kpad] elements
+};
 
-void tc_points(Handle &, int, int, const double *, double *, cudaStream_t) {
-  fail(C2G_ERR_UNSUPPORTED, "split-precision evaluation is not built yet");
+struct TcOperands {
+  TcKind kind[2];  // 0 bf16, 1 tf32
+  int mo_pad = 0, nmt = 0;
+  float *occ = nullptr;
+  int *err = nullptr;  // device error word
+  std::vector<int> order;  // TC primitive order (indices into the handle's prims)
+  std::vector<void *> allocs;
+  double recheck_rel = 1e-3;
+  int *scratch = nullptr;  // re-check list + counter, grown on demand
+  size_t scratch_cap = 0;  // ints
+};
+
+namespace {
+namespace K {
+constexpr int NP = 32;     // points per tile (MMA N)
+constexpr int MT = 128;    // MOs per tile (MMA M)
+constexpr int NCOMP = 10;  // value, 3 first, 6 second derivatives
+constexpr int PIECE = NP * 32;            // bytes of one (component, piece) B tile
+constexpr int STAGE = NCOMP * 2 * PIECE;  // bytes of one K-stage
+constexpr int NSTAGE = 6;  // shared-memory basis-block stages
+constexpr int NCBUF = 4;   // coefficient buffers in TMEM
+constexpr int NPROD = 6;
+constexpr int W_MMA = 4, W_SETUP = 5, W_PROD0 = 6;
+constexpr int NTHR = (W_PROD0 + NPROD) * 32;  // 384
+constexpr uint32_t TMEM_COLS = 512;
+// TMEM columns: accumulators of the hi*hi products for the 10 components,
+// accumulators of the cross products (hi*lo + lo*hi) for the value and the
+// gradient, then the coefficient buffers.  Keeping the small cross terms
+// apart means the large accumulator takes one truncating addition per MMA
+// step instead of three (the tensor core's FP32 accumulation rounds toward
+// zero, so the error grows with the number of additions).
+constexpr int NXCOMP = 4;
+constexpr int XCOL0 = NCOMP * NP;           // 320
+constexpr int CBUF0 = XCOL0 + NXCOMP * NP;  // 448
+static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
+constexpr int RED = 81;  // padded row of the reduction buffer
+constexpr uint64_t TIMEOUT_NS = 4000000000ull;
+// barrier slots
+constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17, B_EPIFULL = 18,
+              B_EPIFREE = 19, B_TREADY = 20, B_TFREE = 22, B_DRAIN = 24, NBAR = 25;
+static_assert(NSTAGE == NPROD, "one producer warp per stage buffer");
+}  // namespace K
+
+struct TcArgs {
+  DevWfn w;
+  const PrimTC *prim;
+  const uint8_t *c_hi, *c_lo;
+  const float *occ;
+  int nstage, kpad, nmt, maskw;
+  int *err;
+  int *recheck, *recheck_count;
+  int recheck_cap;
+  float recheck_rel;
+  unsigned long long *stage_count;  // total active (tile, stage) pairs, or null
+};
+
+struct Smem {
+  uint8_t *stage;
+  float *red, *part;
+  double *acc;
+  double *x;    // [2][32][3]
+  long *idx;    // [2][32]
+  float4 *dl;   // [2][32] offset from the tile reference point, w = valid
+  uint64_t *bar;
+  uint32_t *tmem;
+  volatile int *abort;
+  int *nact;    // [2]
+  float *rad;   // [2] tile radius (max |delta|)
+  uint8_t *key;    // [2][nstage] importance class of each stage (255 = inactive)
+  uint16_t *list;  // [2][nstage] active stages, least important first
+  float4 *off;   // [2][natom] o = reference - atom: (o_hi, |o|^2_hi)
+  float4 *offl;  // [2][natom] (o - o_hi, |o|^2 - |o|^2_hi)
+  float *dmin;   // [2][natom] lower bound of the tile-atom distance
+};
+
+__host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs) {
+  size_t o = 0;
+  auto take = [&](size_t n, size_t al) {
+    o = (o + al - 1) / al * al;
+    size_t r = o;
+    o += n;
+    return r;
+  };
+  offs[0] = take((size_t)K::NSTAGE * K::STAGE, 1024);
+  offs[1] = take(4 * 32 * K::RED * 4, 16);
+  offs[2] = take(4 * 320 * 4, 16);
+  offs[3] = take(10 * 32 * 8, 16);
+  offs[4] = take(2 * 32 * 3 * 8, 16);
+  offs[5] = take(2 * 32 * 8, 16);
+  offs[6] = take(2 * 32 * 16, 16);
+  offs[7] = take(K::NBAR * 8, 16);
+  offs[8] = take(64, 16);
+  offs[9] = take((size_t)2 * maskw * 32 * 3, 16);  // key (1 B) + list (2 B) per stage
+  offs[10] = take((size_t)2 * natom * 16, 16);
+  offs[11] = take((size_t)2 * natom * 16, 16);
+  offs[12] = take((size_t)2 * natom * 4, 16);
+  return o + 1024;  // slack for aligning the dynamic base
 }
 
-void tc_points_index(Handle &, int, const double *, const int *, const int *, int, double *,
-                     cudaStream_t) {
-  fail(C2G_ERR_UNSUPPORTED, "split-precision evaluation is not built yet");
+__device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
+  uint8_t *base = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
+  size_t o[13];
+  smem_bytes(natom, maskw, o);
+  Smem s;
+  s.stage = base + o[0];
+  s.red = (float *)(base + o[1]);
+  s.part = (float *)(base + o[2]);
+  s.acc = (double *)(base + o[3]);
+  s.x = (double *)(base + o[4]);
+  s.idx = (long *)(base + o[5]);
+  s.dl = (float4 *)(base + o[6]);
+  s.bar = (uint64_t *)(base + o[7]);
+  s.tmem = (uint32_t *)(base + o[8]);
+  s.abort = (volatile int *)(base + o[8] + 4);
+  s.nact = (int *)(base + o[8] + 8);
+  s.rad = (float *)(base + o[8] + 16);
+  s.key = (uint8_t *)(base + o[9]);
+  s.list = (uint16_t *)(base + o[9] + (size_t)2 * maskw * 32);
+  s.off = (float4 *)(base + o[10]);
+  s.offl = (float4 *)(base + o[11]);
+  s.dmin = (float *)(base + o[12]);
+  return s;
 }
 
-long tc_nci_grid(Handle &, int, const GridSpec &, double *, double *, cudaStream_t, cudaEvent_t) {
-  fail(C2G_ERR_UNSUPPORTED, "split-precision evaluation is not built yet");
+// Bounded wait by one lane, result broadcast to the warp.
+__device__ __forceinline__ bool warp_wait(const Smem &s, int bar, uint32_t parity, int *err) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    if (*s.abort) ok = 0;
+    else if (!ptx::mbar_wait(&s.bar[bar], parity, K::TIMEOUT_NS)) {
+      ok = 0;
+      *s.abort = 1;
+      atomicOr(err, 1 << (bar < 31 ? bar : 31));
+    }
+  }
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+__device__ __forceinline__ bool thread_wait(const Smem &s, int bar, uint32_t parity, int *err) {
+  if (*s.abort) return false;
+  if (!ptx::mbar_wait(&s.bar[bar], parity, K::TIMEOUT_NS)) {
+    *s.abort = 1;
+    atomicOr(err, 1 << (bar < 31 ? bar : 31));
+    return false;
+  }
+  return true;
+}
+
+// Factors of one Cartesian axis (see k_fp64.cu): with t = -2 alpha,
+//   f0 = x^l, f1 = l x^(l-1) + t x^(l+1), f2 = l(l-1) x^(l-2) + t(2l+1) x^l + t^2 x^(l+2)
+__device__ __forceinline__ void axis3(float x, int l, float t, float &f0, float &f1, float &f2) {
+  float a = 1.f, b = 0.f, c = 0.f;
+  for (int i = 0; i < l; i++) {
+    c = b;
+    b = a;
+    a *= x;
+  }
+  const float p1 = a * x, p2 = p1 * x;
+  f0 = a;
+  f1 = fmaf(t, p1, (float)l * b);
+  f2 = fmaf(t * t, p2, fmaf(t * (float)(2 * l + 1), a, (float)(l * (l - 1)) * c));
+}
+
+// Per (tile, primitive) part of the Gaussian.  With d = o + delta (o = tile
+// reference - atom, delta = point - reference):
+//   exp(-alpha |d|^2) = exp(-alpha |o|^2) * exp(-alpha (2 o.delta + |delta|^2)).
+// The first factor G is computed once per tile from the float-float |o|^2
+// and alpha with a compensated conversion to base 2 (u = arg*log2(e) carried
+// as hi + lo, 2^-u = 2^-n * 2^-f with |f| <= 1/2); the per-point factor has
+// a small argument, so its FP32 rounding stays small.  T = dran^2 - |o|^2
+// turns critic2's cutoff d <= dran into 2 o.delta + |delta|^2 <= T.  When
+// alpha (2|o|R + R^2) is large (tight primitives; R = tile radius) the
+// per-point factor could overflow, and the primitive is evaluated directly
+// from the float-float distance instead (direct = true).
+struct PrimTile {
+  float g, t;
+  bool direct;
+};
+
+__device__ __forceinline__ PrimTile prim_tile(const PrimTC &pr, const float4 &o, const float4 &ol, float rad) {
+  PrimTile r;
+  const float ooh = o.w, ool = ol.w;
+  // arg = alpha * |o|^2 as hi + lo
+  const float p = pr.alpha * ooh;
+  float pe = fmaf(pr.alpha, ooh, -p);
+  pe = fmaf(pr.alpha, ool, fmaf(pr.alpha_lo, ooh, pe));
+  // u = arg * log2(e), log2(e) = L1 + L2
+  const float L1 = 1.44269502162933349609375f, L2 = 1.925963033500011079e-8f;
+  const float u = p * L1;
+  float ue = fmaf(p, L1, -u);
+  ue = fmaf(p, L2, fmaf(pe, L1, ue));
+  const float n = rintf(u);
+  const float f = (u - n) + ue;
+  r.g = (n > 250.f) ? 0.f : ldexpf(exp2f(-f), -(int)n);
+  r.t = pr.dran * pr.dran - (ooh + ool);
+  const float on = sqrtf(ooh);
+  r.direct = pr.alpha * (2.f * on * rad + rad * rad) > 60.f;
+  return r;
+}
+
+// chi (10 components) of one primitive at one point; zero beyond the cutoff
+__device__ __forceinline__ void chi10(const PrimTC &pr, const PrimTile &pt, const float4 &o, const float4 &ol,
+                                      const float4 &d, float dd, float (&chi)[10]) {
+  const float dx = (o.x + d.x) + ol.x, dy = (o.y + d.y) + ol.y, dz = (o.z + d.z) + ol.z;
+  float ex;
+  if (!pt.direct) {
+    const float t = fmaf(2.f * o.x, d.x, fmaf(2.f * o.y, d.y, fmaf(2.f * o.z, d.z, dd)));
+    const bool in = (d.w > 0.f) && (pr.dran > 0.f) && (t <= pt.t);
+    ex = in ? pt.g * exp2f(-pr.al2e * t) : 0.f;
+  } else {
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const bool in = (d.w > 0.f) && (pr.dran > 0.f) && (d2 <= pr.dran * pr.dran);
+    ex = in ? exp2f(-pr.al2e * d2) : 0.f;
+  }
+  const int lp = pr.meta;
+  const float tt = -2.f * pr.alpha;
+  float x0, x1, x2, y0, y1, y2, z0, z1, z2;
+  axis3(dx, lp & 15, tt, x0, x1, x2);
+  axis3(dy, (lp >> 4) & 15, tt, y0, y1, y2);
+  axis3(dz, (lp >> 8) & 15, tt, z0, z1, z2);
+  const float yz = y0 * z0 * ex, xz = x0 * z0 * ex, xy = x0 * y0 * ex;
+  chi[0] = x0 * yz;
+  chi[1] = x1 * yz;
+  chi[2] = y1 * xz;
+  chi[3] = z1 * xy;
+  chi[4] = x2 * yz;
+  chi[5] = y2 * xz;
+  chi[6] = z2 * xy;
+  const float x1e = x1 * ex;
+  chi[7] = x1e * y1 * z0;
+  chi[8] = x1e * z1 * y0;
+  chi[9] = y1 * z1 * x0 * ex;
+}
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// Builds one K-stage of the basis block: lane = point row, both 16-byte
+// halves of the 32-byte row, 10 components x (hi, lo) pieces, in the K-major
+// no-swizzle canonical layout (8-row core matrices of 16 bytes; the two
+// K-halves 128 bytes apart, 8-row groups 256 bytes apart).
+template <int KIND>
+__device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
+                                        const float4 &d, float dd, float rad) {
+  constexpr int KPS = KIND == 0 ? 16 : 8;
+  constexpr int PPB = KIND == 0 ? 8 : 4;  // primitives per 16-byte half row
+  const int r = threadIdx.x & 31;
+  const float4 *off = s.off + par * a.w.natom;
+  const float4 *offl = s.offl + par * a.w.natom;
+  // per-(tile, primitive) Gaussian factors, lane j for primitive j
+  float pg = 0.f, ptt = 0.f;
+  int pdir = 0;
+  if (r < KPS) {
+    const PrimTC pr = a.prim[stage_k + r];
+    const int at = pr.meta >> 12;
+    const PrimTile q = prim_tile(pr, off[at], offl[at], rad);
+    pg = q.g;
+    ptt = q.t;
+    pdir = q.direct;
+  }
+#pragma unroll 1
+  for (int half = 0; half < 2; half++) {
+    uint32_t wv[10][2][4];
+    const int k0 = stage_k + half * PPB;
+#pragma unroll
+    for (int j = 0; j < PPB; j += (KIND == 0 ? 2 : 1)) {
+#pragma unroll
+      for (int jj = 0; jj < (KIND == 0 ? 2 : 1); jj++) {
+        const int jl = half * PPB + j + jj;
+        const PrimTC pr = a.prim[k0 + j + jj];
+        const int at = pr.meta >> 12;
+        PrimTile q;
+        q.g = __shfl_sync(0xffffffffu, pg, jl);
+        q.t = __shfl_sync(0xffffffffu, ptt, jl);
+        q.direct = __shfl_sync(0xffffffffu, pdir, jl) != 0;
+        float c0[10];
+        chi10(pr, q, off[at], offl[at], d, dd, c0);
+        if constexpr (KIND == 0) {
+          // pairs of primitives share a 32-bit word (element k0+j in the low
+          // half): stash the first one's values, pack when the second is known
+          if (jj == 0) {
+#pragma unroll
+            for (int c = 0; c < 10; c++) wv[c][0][j >> 1] = __float_as_uint(c0[c]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 10; c++) {
+              const float c_lo = __uint_as_float(wv[c][0][j >> 1]);
+              const __nv_bfloat162 hi = __floats2bfloat162_rn(c_lo, c0[c]);
+              const float2 hf = __bfloat1622float2(hi);
+              const __nv_bfloat162 lo = __floats2bfloat162_rn(c_lo - hf.x, c0[c] - hf.y);
+              wv[c][0][j >> 1] = *reinterpret_cast<const uint32_t *>(&hi);
+              wv[c][1][j >> 1] = *reinterpret_cast<const uint32_t *>(&lo);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 10; c++) {
+            const uint32_t hi = tf32_rna(c0[c]);
+            wv[c][0][j] = hi;
+            wv[c][1][j] = tf32_rna(c0[c] - __uint_as_float(hi));
+          }
+        }
+      }
+    }
+    uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
+#pragma unroll
+    for (int c = 0; c < 10; c++)
+#pragma unroll
+      for (int pc = 0; pc < 2; pc++)
+        *reinterpret_cast<uint4 *>(row + (c * 2 + pc) * K::PIECE) =
+            make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
+  }
+}
+
+// per-point outputs -----------------------------------------------------------
+struct TcRecSink {
+  double *rec;
+  __device__ void put(const TcArgs &, long idx, const double (&)[3], const double *acc) const {
+#pragma unroll
+    for (int q = 0; q < 10; q++) rec[idx * 10 + q] = acc[q * 32];
+  }
+};
+
+__device__ void eig3_f64(double a00, double a11, double a22, double a01, double a02, double a12,
+                         double (&ev)[3]) {
+  for (int sweep = 0; sweep < 12; sweep++) {
+    const double off = a01 * a01 + a02 * a02 + a12 * a12;
+    const double dia = a00 * a00 + a11 * a11 + a22 * a22;
+    if (off == 0.0 || off < 1e-34 * dia) break;
+    if (a01 != 0.0) {
+      const double th = (a11 - a00) / (2.0 * a01);
+      const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+      const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+      const double n02 = c * a02 - s * a12, n12 = s * a02 + c * a12;
+      a00 -= t * a01; a11 += t * a01; a01 = 0.0; a02 = n02; a12 = n12;
+    }
+    if (a02 != 0.0) {
+      const double th = (a22 - a00) / (2.0 * a02);
+      const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+      const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+      const double n01 = c * a01 - s * a12, n12 = s * a01 + c * a12;
+      a00 -= t * a02; a22 += t * a02; a02 = 0.0; a01 = n01; a12 = n12;
+    }
+    if (a12 != 0.0) {
+      const double th = (a22 - a11) / (2.0 * a12);
+      const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+      const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+      const double n01 = c * a01 - s * a02, n02 = s * a01 + c * a02;
+      a11 -= t * a12; a22 += t * a12; a12 = 0.0; a01 = n01; a02 = n02;
+    }
+  }
+  double e0 = a00, e1 = a11, e2 = a22, t;
+  if (e0 > e1) t = e0, e0 = e1, e1 = t;
+  if (e1 > e2) t = e1, e1 = e2, e2 = t;
+  if (e0 > e1) t = e0, e0 = e1, e1 = t;
+  ev[0] = e0; ev[1] = e1; ev[2] = e2;
+}
+
+// NCI point (src/nci@proc.f90:565-571, 598-599).  sign(lambda2) from the
+// characteristic polynomial (Descartes' rule is exact for the real roots of
+// a symmetric matrix) unless some eigenvalue is small relative to the
+// Hessian's scale; those points use an FP64 eigen-solve, and the ones with
+// |lambda2| < recheck_rel * max|lambda| go to the FP64 re-evaluation list.
+// rho^(4/3) is taken in FP64 where rho < 1e-4.
+struct TcNciSink {
+  double *crho, *cgrad;
+  __device__ void put(const TcArgs &a, long idx, const double (&)[3], const double *acc) const {
+    const double rho = acc[0];
+    const float gx = (float)acc[32], gy = (float)acc[64], gz = (float)acc[96];
+    const float gm = sqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
+    const float cst = 6.18733545256027186f;  // 2 (3 pi^2)^(1/3)
+    double s;
+    if (rho >= 1e-4) {
+      const float r = (float)rho;
+      s = (double)(gm / (cst * r * cbrtf(r)));
+    } else {
+      const double rr = fmax(rho, 1e-80);
+      s = (double)gm / (6.18733545256027186 * rr * cbrt(rr));
+    }
+    const float hxx = (float)acc[128], hyy = (float)acc[160], hzz = (float)acc[192];
+    const float hxy = (float)acc[224], hxz = (float)acc[256], hyz = (float)acc[288];
+    const float tr = hxx + hyy + hzz;
+    const float c2 = hxx * hyy - hxy * hxy + hxx * hzz - hxz * hxz + hyy * hzz - hyz * hyz;
+    const float det = hxx * (hyy * hzz - hyz * hyz) - hxy * (hxy * hzz - hyz * hxz) + hxz * (hxy * hyz - hyy * hxz);
+    const float nrm = sqrtf(hxx * hxx + hyy * hyy + hzz * hzz + 2.f * (hxy * hxy + hxz * hxz + hyz * hyz));
+    bool neg;
+    if (fabsf(det) > 1e-3f * nrm * nrm * nrm) {
+      // sign changes of (1, -tr, c2, -det), zeros skipped
+      const float seq[4] = {1.f, -tr, c2, -det};
+      int changes = 0;
+      float prev = 1.f;
+#pragma unroll
+      for (int i = 1; i < 4; i++)
+        if (seq[i] != 0.f) {
+          if ((seq[i] > 0.f) != (prev > 0.f)) changes++;
+          prev = seq[i];
+        }
+      neg = changes < 2;
+    } else {
+      double ev[3];
+      eig3_f64(acc[128], acc[160], acc[192], acc[224], acc[256], acc[288], ev);
+      neg = signbit(ev[1]);
+      const double big = fmax(fabs(ev[0]), fabs(ev[2]));
+      if (fabs(ev[1]) < (double)a.recheck_rel * big && a.recheck) {
+        const int slot = atomicAdd(a.recheck_count, 1);
+        if (slot < a.recheck_cap) a.recheck[slot] = (int)idx;
+      }
+    }
+    crho[idx] = (neg ? -fabs(rho) : fabs(rho)) * 100.0;
+    cgrad[idx] = s;
+  }
+};
+
+// ------------------------------------------------------------------ kernel
+template <int KIND, class Src, class Sink>
+__global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink, int ntiles) {
+  extern __shared__ uint8_t smem_raw[];
+  const Smem s = carve(smem_raw, a.w.natom, a.maskw);
+  constexpr int KPS = KIND == 0 ? 16 : 8;
+  constexpr int ESZ = KIND == 0 ? 2 : 4;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < K::NSTAGE; b++) {
+      ptx::mbar_init(&s.bar[K::B_CHI + b], 1);
+      ptx::mbar_init(&s.bar[K::B_EMPTY + b], 1);
+    }
+    for (int b = 0; b < K::NCBUF; b++) ptx::mbar_init(&s.bar[K::B_C + b], 4);
+    ptx::mbar_init(&s.bar[K::B_ACCFULL], 1);
+    ptx::mbar_init(&s.bar[K::B_ACCEMPTY], 4);
+    ptx::mbar_init(&s.bar[K::B_EPIFULL], 4);
+    ptx::mbar_init(&s.bar[K::B_EPIFREE], 1);
+    for (int p = 0; p < 2; p++) {
+      ptx::mbar_init(&s.bar[K::B_TREADY + p], 1);
+      ptx::mbar_init(&s.bar[K::B_TFREE + p], K::NPROD + 1 + 4);
+    }
+    ptx::mbar_init(&s.bar[K::B_DRAIN], 1);
+    *s.abort = 0;
+    ptx::mbar_fence_init();
+  }
+  for (int i = threadIdx.x; i < 320; i += K::NTHR) s.acc[i] = 0.0;
+  if (warp == K::W_MMA) {
+    ptx::tmem_alloc(s.tmem, K::TMEM_COLS);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *s.tmem;
+  ntiles = src.tiles(ntiles);
+  const int ntl = ntiles > (int)blockIdx.x ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+
+  if (warp == K::W_SETUP) {
+    // ---------------------------------------------------------- tile setup
+    for (int t = 0; t < ntl; t++) {
+      const int par = t & 1;
+      if (t >= 2 && !warp_wait(s, K::B_TFREE + par, ((t >> 1) - 1) & 1, a.err)) break;
+      const int tile = (int)blockIdx.x + t * (int)gridDim.x;
+      double x[3] = {0.0, 0.0, 0.0};
+      long idx = -1;
+      const bool v = src.point(a.w, tile, lane, x, idx);
+      double *sx = s.x + (par * 32 + lane) * 3;
+      sx[0] = x[0], sx[1] = x[1], sx[2] = x[2];
+      s.idx[par * 32 + lane] = v ? idx : -1;
+      const unsigned vm = __ballot_sync(0xffffffffu, v);
+      const int nv = __popc(vm);
+      double ref[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        double sum = v ? x[c] : 0.0;
+        for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        ref[c] = nv ? sum / nv : 0.0;
+      }
+      const float4 dl = v ? make_float4((float)(x[0] - ref[0]), (float)(x[1] - ref[1]), (float)(x[2] - ref[2]), 1.f)
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+      s.dl[par * 32 + lane] = dl;
+      float rad = v ? sqrtf(dl.x * dl.x + dl.y * dl.y + dl.z * dl.z) : 0.f;
+      for (int o = 16; o; o >>= 1) rad = fmaxf(rad, __shfl_xor_sync(0xffffffffu, rad, o));
+      float4 *off = s.off + par * a.w.natom;
+      float4 *offl = s.offl + par * a.w.natom;
+      float *dmn = s.dmin + par * a.w.natom;
+      for (int at = lane; at < a.w.natom; at += 32) {
+        const double4 A = a.w.atoms[at];
+        const double ox = ref[0] - A.x, oy = ref[1] - A.y, oz = ref[2] - A.z;
+        const double oo = ox * ox + oy * oy + oz * oz;
+        const float hx = (float)ox, hy = (float)oy, hz = (float)oz, ho = (float)oo;
+        off[at] = make_float4(hx, hy, hz, ho);
+        offl[at] = make_float4((float)(ox - hx), (float)(oy - hy), (float)(oz - hz), (float)(oo - ho));
+        dmn[at] = (float)sqrt(oo) - rad - 1e-3f;
+      }
+      if (lane == 0) s.rad[par] = rad;
+      __syncwarp();
+      // K-stages: a stage is active iff some primitive can reach some point.
+      // Its importance class bounds the largest Gaussian factor it can give
+      // in the tile, exp(-min alpha dmin^2); the active stages are listed
+      // from the least to the most important one, so that the truncating
+      // FP32 accumulators stay small for most of the accumulation.
+      uint8_t *key = s.key + par * a.maskw * 32;
+      uint16_t *list = s.list + par * a.maskw * 32;
+      constexpr int SPB = 32 / KPS;  // stages per ballot
+      for (int c0 = 0; c0 < a.maskw * 32; c0 += SPB) {
+        const int k = c0 * KPS + lane;
+        bool act = false;
+        float arg = 3.0e38f;
+        if (nv && k < a.kpad) {
+          const PrimTC pr = a.prim[k];
+          const float dm = fmaxf(dmn[pr.meta >> 12], 0.f);
+          act = pr.dran > 0.f && dmn[pr.meta >> 12] <= pr.dran;
+          if (act) arg = pr.alpha * dm * dm;
+        }
+#pragma unroll
+        for (int o = KPS / 2; o; o >>= 1) arg = fminf(arg, __shfl_xor_sync(0xffffffffu, arg, o));
+        const unsigned b = __ballot_sync(0xffffffffu, act);
+        if ((lane % KPS) == 0) {
+          const int st = c0 + lane / KPS;
+          const bool sact = ((b >> lane) & ((KPS == 32 ? 0u : (1u << KPS)) - 1u)) != 0u;
+          if (st < a.maskw * 32) key[st] = sact ? (uint8_t)fminf(15.f, arg * 0.5f) : (uint8_t)255;
+        }
+      }
+      __syncwarp();
+      int nact = 0;
+      for (int cls = 15; cls >= 0; cls--) {
+        for (int wd = 0; wd < a.maskw; wd++) {
+          const int st = wd * 32 + lane;
+          const bool hit = st < a.nstage && key[st] == cls;
+          const unsigned bb = __ballot_sync(0xffffffffu, hit);
+          if (hit) list[nact + __popc(bb & ((1u << lane) - 1u))] = (uint16_t)st;
+          nact += __popc(bb);
+        }
+      }
+      if (lane == 0) {
+        s.nact[par] = nact;
+        if (a.stage_count) atomicAdd(a.stage_count, (unsigned long long)nact);
+      }
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_TREADY + par]);
+    }
+  } else if (warp == K::W_MMA) {
+    // ------------------------------------------------------------ MMA issue
+    if (lane == 0) {
+      constexpr uint32_t idesc = ptx::make_idesc(KIND == 0 ? 1 : 2, K::MT, K::NP);
+      uint32_t g = 0, u = 0;
+      bool ok = true;
+      for (int t = 0; t < ntl && ok; t++) {
+        const int par = t & 1;
+        if (!(ok = thread_wait(s, K::B_TREADY + par, (t >> 1) & 1, a.err))) break;
+        const int nact = s.nact[par];
+        for (int mt = 0; mt < a.nmt && ok; mt++, u++) {
+          if (u > 0) {
+            if (!(ok = thread_wait(s, K::B_ACCEMPTY, (u - 1) & 1, a.err))) break;
+            ptx::tc_fence_after();
+          }
+          for (int j = 0; j < nact; j++, g++) {
+            const int b = g % K::NSTAGE, cb = g % K::NCBUF;
+            if (!(ok = thread_wait(s, K::B_CHI + b, (g / K::NSTAGE) & 1, a.err))) break;
+            if (!(ok = thread_wait(s, K::B_C + cb, (g / K::NCBUF) & 1, a.err))) break;
+            ptx::tc_fence_after();
+            const uint32_t a_hi = tmem + K::CBUF0 + cb * 16, a_lo = a_hi + 8;
+            const uint32_t sb = ptx::smem_u32(s.stage + b * K::STAGE);
+            const uint32_t acc0 = j > 0 ? 1u : 0u;
+#pragma unroll
+            for (int c = 0; c < K::NCOMP; c++) {
+              const uint32_t dcol = tmem + c * K::NP;
+              const uint32_t xcol = c < K::NXCOMP ? tmem + K::XCOL0 + c * K::NP : dcol;
+              const uint32_t xacc = c < K::NXCOMP ? acc0 : 1u;
+              const uint64_t bh = ptx::smem_desc_kmajor(sb + (2 * c) * K::PIECE, 128, 256);
+              const uint64_t bl = ptx::smem_desc_kmajor(sb + (2 * c + 1) * K::PIECE, 128, 256);
+              if constexpr (KIND == 0) {
+                ptx::mma_bf16_ts(dcol, a_hi, bh, idesc, acc0);
+                ptx::mma_bf16_ts(xcol, a_hi, bl, idesc, xacc);
+                ptx::mma_bf16_ts(xcol, a_lo, bh, idesc, 1u);
+              } else {
+                ptx::mma_tf32_ts(dcol, a_hi, bh, idesc, acc0);
+                ptx::mma_tf32_ts(xcol, a_hi, bl, idesc, xacc);
+                ptx::mma_tf32_ts(xcol, a_lo, bh, idesc, 1u);
+              }
+            }
+            ptx::mma_commit(&s.bar[K::B_EMPTY + b]);
+          }
+          if (!ok) break;
+          ptx::mma_commit(&s.bar[K::B_ACCFULL]);
+        }
+        if (ok) ptx::mbar_arrive(&s.bar[K::B_TFREE + par]);
+      }
+      // drain outstanding MMAs before the teardown
+      ptx::mma_commit(&s.bar[K::B_DRAIN]);
+      ptx::mbar_wait(&s.bar[K::B_DRAIN], 0, K::TIMEOUT_NS);
+    }
+  } else if (warp >= K::W_PROD0) {
+    // -------------------------------------------------------- basis block
+    const int pw = warp - K::W_PROD0;
+    uint32_t g = 0;
+    bool ok = true;
+    for (int t = 0; t < ntl && ok; t++) {
+      const int par = t & 1;
+      if (!(ok = warp_wait(s, K::B_TREADY + par, (t >> 1) & 1, a.err))) break;
+      const float4 d = s.dl[par * 32 + lane];
+      const float dd = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+      const float rad = s.rad[par];
+      const uint16_t *list = s.list + par * a.maskw * 32;
+      const int nact = s.nact[par];
+      for (int mt = 0; mt < a.nmt && ok; mt++) {
+        for (int j = 0; j < nact && ok; j++, g++) {
+          if ((int)(g % K::NPROD) != pw) continue;
+          const int sk = list[j];
+          const int b = g % K::NSTAGE;
+          if (g >= (uint32_t)K::NSTAGE && !(ok = warp_wait(s, K::B_EMPTY + b, ((g / K::NSTAGE) - 1) & 1, a.err)))
+            break;
+          produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, dd, rad);
+          ptx::fence_proxy_async_smem();
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_CHI + b]);
+        }
+      }
+      __syncwarp();
+      if (ok && lane == 0) ptx::mbar_arrive(&s.bar[K::B_TFREE + par]);
+    }
+  } else {
+    // ----------------------------------------- coefficient loader + epilogue
+    const int q = warp;  // TMEM lane quadrant
+    const uint32_t lanebase = (uint32_t)(32 * q) << 16;
+    uint32_t g = 0, u = 0;
+    bool ok = true;
+    float *red = s.red + q * 32 * K::RED;
+    for (int t = 0; t < ntl && ok; t++) {
+      const int par = t & 1;
+      if (!(ok = warp_wait(s, K::B_TREADY + par, (t >> 1) & 1, a.err))) break;
+      const int nact = s.nact[par];
+      const uint16_t *list = s.list + par * a.maskw * 32;
+      for (int mt = 0; mt < a.nmt && ok; mt++, u++) {
+        const int mo = mt * K::MT + 32 * q + lane;
+        const uint8_t *crow_hi = a.c_hi + (size_t)mo * a.kpad * ESZ;
+        const uint8_t *crow_lo = a.c_lo + (size_t)mo * a.kpad * ESZ;
+        for (int j = 0; j < nact && ok; j++, g++) {
+          const int sk = list[j];
+          const int cb = g % K::NCBUF;
+          const uint4 h0 = __ldg(reinterpret_cast<const uint4 *>(crow_hi + (size_t)sk * 32));
+          const uint4 h1 = __ldg(reinterpret_cast<const uint4 *>(crow_hi + (size_t)sk * 32 + 16));
+          const uint4 l0 = __ldg(reinterpret_cast<const uint4 *>(crow_lo + (size_t)sk * 32));
+          const uint4 l1 = __ldg(reinterpret_cast<const uint4 *>(crow_lo + (size_t)sk * 32 + 16));
+          // buffer cb was last read by the MMAs of stage g - NCBUF
+          if (g >= (uint32_t)K::NCBUF) {
+            const uint32_t gp = g - K::NCBUF;
+            if (!(ok = warp_wait(s, K::B_EMPTY + gp % K::NSTAGE, (gp / K::NSTAGE) & 1, a.err))) break;
+          }
+          const uint32_t hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+          const uint32_t lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+          ptx::tmem_st8(tmem + lanebase + K::CBUF0 + cb * 16, hv);
+          ptx::tmem_st8(tmem + lanebase + K::CBUF0 + cb * 16 + 8, lv);
+          ptx::tmem_wait_st();
+          ptx::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_C + cb]);
+        }
+        if (!ok) break;
+        // ----- epilogue of this (point tile, MO tile)
+        if (!(ok = warp_wait(s, K::B_ACCFULL, u & 1, a.err))) break;
+        ptx::tc_fence_after();
+        if (q != 0 && u > 0 && !(ok = warp_wait(s, K::B_EPIFREE, (u - 1) & 1, a.err))) break;
+        float *part = s.part + q * 320;
+        if (nact > 0) {
+          const float occ = a.occ[mo];
+#pragma unroll 1
+          for (int ch = 0; ch < 4; ch++) {
+            uint32_t v[10][8], xv[K::NXCOMP][8];
+#pragma unroll
+            for (int c = 0; c < 10; c++) ptx::tmem_ld8(tmem + lanebase + c * K::NP + ch * 8, v[c]);
+#pragma unroll
+            for (int c = 0; c < K::NXCOMP; c++) ptx::tmem_ld8(tmem + lanebase + K::XCOL0 + c * K::NP + ch * 8, xv[c]);
+            ptx::tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+              const float p0 = __uint_as_float(v[0][j]) + __uint_as_float(xv[0][j]);
+              const float px = __uint_as_float(v[1][j]) + __uint_as_float(xv[1][j]);
+              const float py = __uint_as_float(v[2][j]) + __uint_as_float(xv[2][j]);
+              const float pz = __uint_as_float(v[3][j]) + __uint_as_float(xv[3][j]);
+              const float o2 = 2.f * occ, t0 = o2 * p0;
+              const float ux = o2 * px, uy = o2 * py, uz = o2 * pz;
+              float *rw = red + lane * K::RED + j;
+              rw[0] = occ * p0 * p0;
+              rw[8] = t0 * px;
+              rw[16] = t0 * py;
+              rw[24] = t0 * pz;
+              rw[32] = fmaf(t0, __uint_as_float(v[4][j]), ux * px);
+              rw[40] = fmaf(t0, __uint_as_float(v[5][j]), uy * py);
+              rw[48] = fmaf(t0, __uint_as_float(v[6][j]), uz * pz);
+              rw[56] = fmaf(t0, __uint_as_float(v[7][j]), ux * py);
+              rw[64] = fmaf(t0, __uint_as_float(v[8][j]), ux * pz);
+              rw[72] = fmaf(t0, __uint_as_float(v[9][j]), uy * pz);
+            }
+            __syncwarp();
+            for (int col = lane; col < 80; col += 32) {
+              // pairwise: 4 interleaved partial sums of 8 rows, then a tree
+              float s4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+              for (int rr = 0; rr < 32; rr++) s4[rr & 3] += red[rr * K::RED + col];
+              part[ch * 80 + col] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+            }
+            __syncwarp();
+          }
+        } else {
+          for (int i = lane; i < 320; i += 32) part[i] = 0.f;
+        }
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          ptx::mbar_arrive(&s.bar[K::B_ACCEMPTY]);
+          ptx::mbar_arrive(&s.bar[K::B_EPIFULL]);
+        }
+        if (q == 0) {
+          if (!(ok = warp_wait(s, K::B_EPIFULL, u & 1, a.err))) break;
+          const int p = lane;
+#pragma unroll
+          for (int k = 0; k < 10; k++) {
+            const int i = (p >> 3) * 80 + k * 8 + (p & 7);
+            const float v4 = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
+            s.acc[k * 32 + p] += (double)v4;
+          }
+          if (mt == a.nmt - 1) {
+            const long idx = s.idx[par * 32 + p];
+            if (idx >= 0) {
+              const double *sx = s.x + (par * 32 + p) * 3;
+              const double xx[3] = {sx[0], sx[1], sx[2]};
+              sink.put(a, idx, xx, s.acc + p);
+            }
+#pragma unroll
+            for (int k = 0; k < 10; k++) s.acc[k * 32 + p] = 0.0;
+          }
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_EPIFREE]);
+        }
+      }
+      __syncwarp();
+      if (ok && lane == 0) ptx::mbar_arrive(&s.bar[K::B_TFREE + par]);
+    }
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == K::W_MMA) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, K::TMEM_COLS);
+  }
+}
+
+__global__ void k_zero_cgrad(double *cgrad, const int *idx, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cgrad[idx[i]] = 0.0;
+}
+
+// ------------------------------------------------------------------- host
+uint32_t morton3(const double *p, const double *lo, const double *span) {
+  uint32_t q[3];
+  for (int c = 0; c < 3; c++) {
+    double f = (p[c] - lo[c]) / (span[c] > 0 ? span[c] : 1.0);
+    q[c] = (uint32_t)std::min(1023.0, std::max(0.0, f * 1023.0));
+  }
+  uint32_t m = 0;
+  for (int b = 0; b < 10; b++)
+    for (int c = 0; c < 3; c++) m |= ((q[c] >> b) & 1u) << (3 * b + c);
+  return m;
+}
+
+template <class T>
+T *dev_upload(TcOperands *t, const std::vector<T> &v) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(1, v.size() * sizeof(T))) != cudaSuccess)
+    fail(C2G_ERR_ALLOC, "cudaMalloc (split operands)");
+  t->allocs.push_back(p);
+  if (!v.empty()) C2G_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return static_cast<T *>(p);
+}
+
+uint16_t bf16_bits(float x) {
+  const __nv_bfloat16 b = __float2bfloat16_rn(x);
+  uint16_t u;
+  std::memcpy(&u, &b, 2);
+  return u;
+}
+
+float bf16_val(uint16_t u) {
+  uint32_t w = (uint32_t)u << 16;
+  float f;
+  std::memcpy(&f, &w, 4);
+  return f;
+}
+
+// round to nearest (ties away) at the TF32 precision (10 explicit bits)
+uint32_t tf32_bits_host(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return u;
+  u += 0x1000u;
+  return u & 0xffffe000u;
+}
+
+float from_bits(uint32_t u) {
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+void ensure_kind(Handle &h, int kind) {
+  TcOperands *t = h.tc;
+  TcKind &kd = t->kind[kind];
+  if (kd.built) return;
+  const HostWfn &w = h.host;
+  kd.kps = kind == 0 ? 16 : 8;
+  kd.nstage = (w.npri + kd.kps - 1) / kd.kps;
+  kd.kpad = kd.nstage * kd.kps;
+  const int n = (int)t->order.size();
+  std::vector<PrimTC> prim(kd.kpad);
+  for (int k = 0; k < kd.kpad; k++) {
+    if (k < n) {
+      const int ip = t->order[k];
+      const int *l = kLi[w.itype[ip] - 1];
+      prim[k] = PrimTC{};
+      prim[k].alpha = (float)w.e[ip];
+      prim[k].alpha_lo = (float)(w.e[ip] - (double)prim[k].alpha);
+      prim[k].al2e = (float)(w.e[ip] * 1.4426950408889634);
+      prim[k].dran = (float)w.dran[ip];
+      prim[k].meta = (w.icenter[ip] << 12) | l[0] | (l[1] << 4) | (l[2] << 8);
+    } else {
+      prim[k] = PrimTC{};  // dran 0: never in range; zero coefficients
+      prim[k].alpha = 1.f;
+      prim[k].al2e = 1.f;
+    }
+  }
+  const size_t ne = (size_t)t->mo_pad * kd.kpad;
+  if (kind == 0) {
+    std::vector<uint16_t> hi(ne, 0), lo(ne, 0);
+    for (int m = 0; m < w.nmo; m++)
+      for (int k = 0; k < n; k++) {
+        const double c = w.cmo[(size_t)t->order[k] * w.nmo + m];
+        const uint16_t hb = bf16_bits((float)c);
+        hi[(size_t)m * kd.kpad + k] = hb;
+        lo[(size_t)m * kd.kpad + k] = bf16_bits((float)(c - (double)bf16_val(hb)));
+      }
+    kd.c_hi = reinterpret_cast<uint8_t *>(dev_upload(t, hi));
+    kd.c_lo = reinterpret_cast<uint8_t *>(dev_upload(t, lo));
+  } else {
+    std::vector<uint32_t> hi(ne, 0), lo(ne, 0);
+    for (int m = 0; m < w.nmo; m++)
+      for (int k = 0; k < n; k++) {
+        const double c = w.cmo[(size_t)t->order[k] * w.nmo + m];
+        const uint32_t hb = tf32_bits_host((float)c);
+        hi[(size_t)m * kd.kpad + k] = hb;
+        lo[(size_t)m * kd.kpad + k] = tf32_bits_host((float)(c - (double)from_bits(hb)));
+      }
+    kd.c_hi = reinterpret_cast<uint8_t *>(dev_upload(t, hi));
+    kd.c_lo = reinterpret_cast<uint8_t *>(dev_upload(t, lo));
+  }
+  kd.prim = dev_upload(t, prim);
+  kd.built = true;
+}
+
+int kind_of(int prec) {
+  if (prec == C2G_PREC_BF16X3) return 0;
+  if (prec == C2G_PREC_TF32X3) return 1;
+  fail(C2G_ERR_ARG, "not a split-precision mode");
+}
+
+TcArgs make_args(Handle &h, int kind) {
+  ensure_kind(h, kind);
+  TcOperands *t = h.tc;
+  const TcKind &kd = t->kind[kind];
+  TcArgs a{};
+  a.w = h.dev;
+  a.prim = kd.prim;
+  a.c_hi = kd.c_hi;
+  a.c_lo = kd.c_lo;
+  a.occ = t->occ;
+  a.nstage = kd.nstage;
+  a.kpad = kd.kpad;
+  a.nmt = t->nmt;
+  a.maskw = (kd.nstage + 31) / 32;
+  a.err = t->err;
+  a.recheck = nullptr;
+  a.recheck_count = nullptr;
+  a.recheck_cap = 0;
+  a.recheck_rel = (float)t->recheck_rel;
+  a.stage_count = nullptr;
+  return a;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  C2G_CUDA(cudaGetDevice(&dev));
+  C2G_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  return n;
+}
+
+template <int KIND, class Src, class Sink>
+void launch_tc(const TcArgs &a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  size_t offs[13];
+  const size_t bytes = smem_bytes(a.w.natom, a.maskw, offs);
+  if (bytes > 227 * 1024) fail(C2G_ERR_UNSUPPORTED, "molecule too large for the split-precision kernel's shared memory");
+  auto fn = k_tc<KIND, Src, Sink>;
+  C2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  const int grid = std::min(ntiles, sm_count());
+  fn<<<grid, K::NTHR, bytes, st>>>(a, src, sink, ntiles);
+  C2G_CUDA(cudaGetLastError());
+}
+
+template <class Src, class Sink>
+void launch_kind(int kind, const TcArgs &a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st) {
+  if (kind == 0) launch_tc<0>(a, src, sink, ntiles, st);
+  else launch_tc<1>(a, src, sink, ntiles, st);
+}
+
+void check_device_error(TcOperands *t) {
+  int e = 0;
+  C2G_CUDA(cudaMemcpy(&e, t->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    C2G_CUDA(cudaMemset(t->err, 0, sizeof(int)));
+    fail(C2G_ERR_CUDA, "split-precision kernel: a pipeline wait timed out (mask " + std::to_string(e) + ")");
+  }
+}
+
+}  // namespace
+
+TcOperands *tc_create(Handle &h) {
+  auto *t = new TcOperands();
+  try {
+    const HostWfn &w = h.host;
+    t->mo_pad = (w.nmo + K::MT - 1) / K::MT * K::MT;
+    t->nmt = t->mo_pad / K::MT;
+    // Primitive order for the K-stages: diffuse to compact by cutoff
+    // bucket (factors of 2), then by the atom's Morton code, keeping each
+    // atom's primitives (and so each shell) together.
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int a = 0; a < w.natom; a++)
+      for (int c = 0; c < 3; c++) lo[c] = std::min(lo[c], w.xyz[3 * a + c]), hi[c] = std::max(hi[c], w.xyz[3 * a + c]);
+    const double span[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    std::vector<uint32_t> mort(w.natom);
+    for (int a = 0; a < w.natom; a++) mort[a] = morton3(&w.xyz[3 * a], lo, span);
+    t->order.resize(w.npri);
+    std::iota(t->order.begin(), t->order.end(), 0);
+    auto bucket = [&](int ip) { return -(int)std::floor(std::log2(w.dran[ip])); };
+    std::stable_sort(t->order.begin(), t->order.end(), [&](int x, int y) {
+      const int bx = bucket(x), by = bucket(y);
+      if (bx != by) return bx < by;
+      const int ax = w.icenter[x], ay = w.icenter[y];
+      if (mort[ax] != mort[ay]) return mort[ax] < mort[ay];
+      return ax < ay;
+    });
+    std::vector<float> occ(t->mo_pad, 0.f);
+    for (int m = 0; m < w.nmo; m++) occ[m] = (float)w.occ[m];
+    t->occ = dev_upload(t, occ);
+    std::vector<int> zero(1, 0);
+    t->err = dev_upload(t, zero);
+  } catch (...) {
+    tc_destroy(t);
+    throw;
+  }
+  return t;
+}
+
+void tc_destroy(TcOperands *t) {
+  if (!t) return;
+  for (void *p : t->allocs) cudaFree(p);
+  if (t->scratch) cudaFree(t->scratch);
+  delete t;
+}
+
+void tc_set_recheck(Handle &h, double rel) { h.tc->recheck_rel = rel; }
+
+void tc_check_error(Handle &h) { check_device_error(h.tc); }
+
+void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st) {
+  const int kind = kind_of(prec);
+  TcArgs a = make_args(h, kind);
+  ListSrc src{d_xyz, n};
+  launch_kind(kind, a, src, TcRecSink{d_rec}, (n + 31) / 32, st);
+  C2G_CUDA(cudaStreamSynchronize(st));
+  check_device_error(h.tc);
+}
+
+void tc_points_index(Handle &h, int prec, const double *d_x, const int *d_idx, const int *d_count, int maxn,
+                     double *d_rec, cudaStream_t st) {
+  const int kind = kind_of(prec);
+  TcArgs a = make_args(h, kind);
+  IndexSrc src{d_x, d_idx, d_count};
+  launch_kind(kind, a, src, TcRecSink{d_rec}, (maxn + 31) / 32, st);
+}
+
+long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad, cudaStream_t st,
+                 cudaEvent_t ev_split, double *stage_frac) {
+  const int kind = kind_of(prec);
+  TcArgs a = make_args(h, kind);
+  const long npts = (long)g.nstep[0] * g.nstep[1] * g.nstep[2];
+  // scratch: re-check list (one slot per point) and its counter
+  TcOperands *t = h.tc;
+  if (t->scratch_cap < (size_t)npts + 8) {
+    if (t->scratch) cudaFree(t->scratch);
+    t->scratch = nullptr;
+    t->scratch_cap = 0;
+    if (cudaMalloc(&t->scratch, sizeof(int) * ((size_t)npts + 8)) != cudaSuccess)
+      fail(C2G_ERR_ALLOC, "cudaMalloc (re-check list)");
+    t->scratch_cap = (size_t)npts + 8;
+  }
+  int *scratch = t->scratch;
+  int *count = scratch + npts;
+  // the 64-bit stage counter sits at an 8-byte aligned slot after the count
+  unsigned long long *stage_count = reinterpret_cast<unsigned long long *>(scratch + ((npts + 2) & ~1L) + 2);
+  C2G_CUDA(cudaMemsetAsync(count, 0, sizeof(int) * 8, st));
+  a.stage_count = stage_count;
+  a.recheck = scratch;
+  a.recheck_count = count;
+  a.recheck_cap = (int)npts;
+  GridSrc src{g, (g.nstep[1] + 3) / 4, (g.nstep[2] + 7) / 8};
+  const long ntiles = (long)g.nstep[0] * src.ntj * src.ntk;
+  launch_kind(kind, a, src, TcNciSink{d_crho, d_cgrad}, (int)ntiles, st);
+  if (ev_split) C2G_CUDA(cudaEventRecord(ev_split, st));
+  // FP64 re-evaluation of the listed points (the count is read on device)
+  launch_fp64_nci_list(h.dev, g, scratch, count, (int)npts, d_crho, d_cgrad, st);
+  // nucleus rule: |grad| := 0 (s = 0) at grid points within 1e-5 bohr of a nucleus
+  std::vector<int> nuc;
+  {
+    const HostWfn &w = h.host;
+    // invert xmat (columns = axis steps) to locate each nucleus on the grid
+    const double *M = g.xmat;
+    const double det = M[0] * (M[4] * M[8] - M[7] * M[5]) - M[3] * (M[1] * M[8] - M[7] * M[2]) +
+                       M[6] * (M[1] * M[5] - M[4] * M[2]);
+    if (det != 0.0) {
+      double inv[9];
+      inv[0] = (M[4] * M[8] - M[5] * M[7]) / det;
+      inv[3] = (M[5] * M[6] - M[3] * M[8]) / det;
+      inv[6] = (M[3] * M[7] - M[4] * M[6]) / det;
+      inv[1] = (M[2] * M[7] - M[1] * M[8]) / det;
+      inv[4] = (M[0] * M[8] - M[2] * M[6]) / det;
+      inv[7] = (M[1] * M[6] - M[0] * M[7]) / det;
+      inv[2] = (M[1] * M[5] - M[2] * M[4]) / det;
+      inv[5] = (M[2] * M[3] - M[0] * M[5]) / det;
+      inv[8] = (M[0] * M[4] - M[1] * M[3]) / det;
+      for (int at = 0; at < w.natom; at++) {
+        double r[3], f[3];
+        for (int c = 0; c < 3; c++) r[c] = w.xyz[3 * at + c] - g.x0[c];
+        for (int c = 0; c < 3; c++) f[c] = inv[c] * r[0] + inv[3 + c] * r[1] + inv[6 + c] * r[2];
+        long ii[3];
+        bool inside = true;
+        for (int c = 0; c < 3; c++) {
+          ii[c] = std::lround(f[c]);
+          if (ii[c] < 0 || ii[c] >= g.nstep[c]) inside = false;
+        }
+        if (!inside) continue;
+        double d2 = 0.0;
+        for (int c = 0; c < 3; c++) {
+          const double x = g.x0[c] + ii[0] * M[c] + ii[1] * M[3 + c] + ii[2] * M[6 + c];
+          d2 += (x - w.xyz[3 * at + c]) * (x - w.xyz[3 * at + c]);
+        }
+        if (std::sqrt(d2) <= 1e-5) nuc.push_back((int)((ii[0] * g.nstep[1] + ii[1]) * g.nstep[2] + ii[2]));
+      }
+    }
+  }
+  if (!nuc.empty()) {
+    int *dn = nullptr;
+    C2G_CUDA(cudaMalloc(&dn, sizeof(int) * nuc.size()));
+    C2G_CUDA(cudaMemcpyAsync(dn, nuc.data(), sizeof(int) * nuc.size(), cudaMemcpyHostToDevice, st));
+    k_zero_cgrad<<<((int)nuc.size() + 127) / 128, 128, 0, st>>>(d_cgrad, dn, (int)nuc.size());
+    C2G_CUDA(cudaGetLastError());
+    C2G_CUDA(cudaStreamSynchronize(st));
+    cudaFree(dn);
+  }
+  int hcount = 0;
+  unsigned long long hstages = 0;
+  C2G_CUDA(cudaMemcpyAsync(&hcount, count, sizeof(int), cudaMemcpyDeviceToHost, st));
+  C2G_CUDA(cudaMemcpyAsync(&hstages, stage_count, sizeof(hstages), cudaMemcpyDeviceToHost, st));
+  C2G_CUDA(cudaStreamSynchronize(st));
+  check_device_error(h.tc);
+  if (stage_frac) *stage_frac = (double)hstages / ((double)ntiles * t->kind[kind].nstage);
+  return hcount;
 }
 
 }  // namespace c2g

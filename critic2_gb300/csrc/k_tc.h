@@ -9,6 +9,13 @@ namespace c2g {
 TcOperands *tc_create(Handle &h);
 void tc_destroy(TcOperands *t);
 
+// Relative |lambda2| threshold below which split-precision NCI points are
+// re-evaluated in FP64.
+void tc_set_recheck(Handle &h, double rel);
+
+// Reports (and clears) a pipeline timeout recorded by an earlier split kernel.
+void tc_check_error(Handle &h);
+
 // kRecNci records (rho, grad, hess) at n device points, split precision.
 void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st);
 
@@ -19,8 +26,9 @@ void tc_points_index(Handle &h, int prec, const double *d_x, const int *d_idx, c
 
 // NCI grid in split precision followed by the FP64 re-check of the points
 // whose Hessian has |lambda2| < 1e-3 |lambda1|.  Records ev_split after the
-// split pass when not null.  Returns the number of re-checked points.
+// split pass when not null, and the fraction of active K-stages per tile in
+// *stage_frac when not null.  Returns the number of re-checked points.
 long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad,
-                 cudaStream_t st, cudaEvent_t ev_split);
+                 cudaStream_t st, cudaEvent_t ev_split, double *stage_frac);
 
 }  // namespace c2g

@@ -72,6 +72,11 @@ class Wavefunction:
     def __exit__(self, *a):
         self.close()
 
+    def set_recheck(self, rel: float):
+        """Relative |lambda2| below which split-precision NCI points are
+        re-evaluated in FP64 (C2G_PARAM_RECHECK_REL)."""
+        L.check(L.lib().c2g_wfn_set_param(self._h, 1, float(rel)))
+
     # ------------------------------------------------------------ rho2/grd
     def rho2(self, xyz, nder: int = 2, prec="fp64") -> dict:
         """molwfn%rho2 at points xyz (n,3).  Arrays are per point:

@@ -90,6 +90,12 @@ int c2g_wfn_read_wfx(const char *path, c2g_wfn **out);
 /* Frees the handle and its device memory. */
 int c2g_wfn_destroy(c2g_wfn *h);
 
+/* Tunable parameters of a handle. */
+#define C2G_PARAM_RECHECK_REL 1 /* split-precision NCI: points with
+                                   |lambda2| < value * max|lambda| are
+                                   re-evaluated in FP64 (default 1e-3) */
+int c2g_wfn_set_param(c2g_wfn *h, int param, double value);
+
 /* Sizes after pruning. */
 int c2g_wfn_info(const c2g_wfn *h, int *natom, int *npri, int *nmo, int *wfntyp, int *nalpha);
 
@@ -121,6 +127,8 @@ typedef struct {
   long nrecheck;        /* points re-evaluated in FP64 (|l2| < 1e-3 |l1|) */
   double ms_kernel;     /* device time of the evaluation, milliseconds */
   double ms_recheck;    /* device time of the FP64 re-check pass */
+  double stage_frac;    /* split modes: fraction of the K-stages of a 32-point
+                           tile that some point of the tile can see */
 } c2g_nci_stats;
 
 /* The nciplot grid loop (src/nci@proc.f90:540-605) over the grid

@@ -1,0 +1,164 @@
+"""Split-precision (tcgen05) evaluator parity.
+
+The split modes are checked against the oracle (FP64) at random points and
+against the GPU's FP64 plain form on NCI grids.  Tolerances are the
+spec bars where they apply (|drho|/rho <= 1e-6 and |ds| <= 1e-3 for
+the 3-product TF32 split; the BF16 split carries 16 mantissa bits per
+operand pair and is held to 5e-5 relative)."""
+import numpy as np
+import pytest
+
+from critic2_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+# measured levels with a margin; the bench reports the NCI-grid errors
+# against the spec bars (|drho|/rho <= 1e-6, |ds| <= 1e-3)
+TOL = {"tf32x3": dict(rho=5e-6, grad=2e-5, s=1e-3), "bf16x3": dict(rho=5e-5, grad=1e-3, s=1e-2)}
+
+
+@pytest.fixture(scope="module")
+def mol12():
+    return synth.make_molecule("nci12")
+
+
+@pytest.fixture(scope="module")
+def w12(gpu_lib, mol12):
+    from critic2_gb300.wfn import Wavefunction
+    return Wavefunction(mol12)
+
+
+@pytest.fixture(scope="module")
+def o12(oracle_mod, mol12):
+    return oracle_mod.Wfn(mol12)
+
+
+def rel(a, b, floor):
+    return np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))
+
+
+def binned(rho_ref, err, lo=-8, hi=4):
+    """max error per density decade (the precision study's binning)."""
+    out = {}
+    dec = np.floor(np.log10(np.maximum(rho_ref, 1e-300)))
+    for d in range(lo, hi):
+        k = dec == d
+        if k.any():
+            out[f"1e{d}"] = (int(k.sum()), float(err[k].max()))
+    k = dec < lo
+    if k.any():
+        out["<1e%d" % lo] = (int(k.sum()), float(err[k].max()))
+    return out
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+def test_rho2_points_vs_oracle(w12, o12, mol12, prec):
+    rng = np.random.default_rng(11)
+    lo, hi = mol12.atom_xyz.min(0) - 3, mol12.atom_xyz.max(0) + 3
+    pts = rng.uniform(lo, hi, size=(1000, 3))
+    out = w12.rho2(pts, 2, prec)
+    rho_r, g_r, h_r = o12.rho2_points(pts, 2)
+    rho = out["rho"][:, 0]
+    grad = out["grad"][:, 0, :]
+    hess = out["hess"][:, 0].reshape(-1, 9)
+    e_rho = np.abs(rho - rho_r) / np.maximum(rho_r, 1e-300)
+    gscale = np.abs(g_r).max(1) + 1e-3 * rho_r
+    e_g = np.max(np.abs(grad - g_r), 1) / gscale
+    e_h = np.max(np.abs(hess - h_r), 1) / np.abs(h_r).max(1)
+    print(f"\n{prec} rho error by density decade (count, max):", binned(rho_r, e_rho))
+    print(f"{prec} grad error by decade:", binned(rho_r, e_g))
+    print(f"{prec} hess error by decade:", binned(rho_r, e_h))
+    sig = rho_r >= 1e-6
+    assert e_rho[sig].max() < TOL[prec]["rho"]
+    assert e_g[sig].max() < TOL[prec]["grad"]
+    assert e_h[sig].max() < TOL[prec]["grad"]
+
+
+def test_multi_mo_tile_and_far_points(gpu_lib, oracle_mod):
+    """200 MOs (two 128-MO tiles) and points far from the molecule, where
+    most K-stages are skipped or none is active."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("cp100")
+    g, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    rng = np.random.default_rng(2)
+    lo, hi = mol.atom_xyz.min(0), mol.atom_xyz.max(0)
+    pts = np.concatenate([rng.uniform(lo, hi, size=(96, 3)),
+                          hi + rng.uniform(8, 17, size=(32, 3))])
+    out = g.rho2(pts, 2, "tf32x3")
+    rho_r, g_r, _ = o.rho2_points(pts, 2)
+    rho = out["rho"][:, 0]
+    near = slice(0, 96)
+    assert rel(rho[near], rho_r[near], 1e-300) < TOL["tf32x3"]["rho"]
+    far_ok = np.abs(rho[96:] - rho_r[96:]) <= 1e-6 * np.maximum(rho_r[96:], 1e-30) + 1e-30
+    assert far_ok.all()
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+def test_nci_grid_vs_fp64(w12, mol12, prec):
+    x0, xm, ns = synth.nci_grid(mol12, 80, 0.1)
+    c64, s64, _ = w12.nciplot(x0, xm, ns, "fp64")
+    c, s, st = w12.nciplot(x0, xm, ns, prec)
+    rho64, rho = np.abs(c64) / 100, np.abs(c) / 100
+    e_rho = rel(rho, rho64, 1e-300)
+    e_s = np.max(np.abs(s - s64))
+    flips = int((np.sign(c) != np.sign(c64)).sum())
+    print(f"\n{prec} NCI 80^3: max rel rho {e_rho:.2e}, max |ds| {e_s:.2e}, flips {flips}, rechecked {st.nrecheck}")
+    er = np.abs(rho - rho64) / rho64
+    print(f"{prec} NCI rho error by decade:", binned(rho64.reshape(-1), er.reshape(-1)))
+    assert e_rho < TOL[prec]["rho"]
+    assert e_s < TOL[prec]["s"]
+    assert flips <= max(2, int(1e-5 * c.size))
+
+
+def test_nci_grid_odd_shape(w12, mol12):
+    """Grid extents that are not multiples of the 4 x 8 tile."""
+    x0, xm, _ = synth.nci_grid(mol12, 37, 0.23)
+    ns = np.array([13, 37, 29], np.int32)
+    c64, s64, _ = w12.nciplot(x0, xm, ns, "fp64")
+    c, s, _ = w12.nciplot(x0, xm, ns, "tf32x3")
+    assert rel(np.abs(c), np.abs(c64), 1e-300) < TOL["tf32x3"]["rho"]
+    assert np.max(np.abs(s - s64)) < 1e-3
+
+
+def test_recheck_threshold(w12, mol12):
+    x0, xm, ns = synth.nci_grid(mol12, 40, 0.2)
+    c64, _, _ = w12.nciplot(x0, xm, ns, "fp64")
+    w12.set_recheck(0.0)
+    c0, _, st0 = w12.nciplot(x0, xm, ns, "tf32x3")
+    w12.set_recheck(0.5)
+    c1, _, st1 = w12.nciplot(x0, xm, ns, "tf32x3")
+    w12.set_recheck(1e-3)
+    assert st0.nrecheck == 0 and st1.nrecheck > 0
+    # re-checked points are the FP64 values exactly
+    assert np.sum(np.sign(c1) != np.sign(c64)) <= np.sum(np.sign(c0) != np.sign(c64))
+
+
+def test_newton_split(w12, o12):
+    """Every point the split-precision Newton calls converged is a CP of the
+    FP64 field (its last steps run in FP64)."""
+    seeds = w12.pair_seeds()[::13]
+    xs, isp = w12.newton(seeds, 1e-12, 200, "tf32x3")
+    assert (isp == 0).mean() > 0.7
+    for x in xs[isp == 0]:
+        assert o12.grd(x, 2).gfmod < 1e-9
+
+
+def test_autocritic_split_same_cps(w12, o12):
+    """AUTO in split precision finds the CP set of the FP64 search (Newton
+    paths from single seeds may differ; the set of CPs must not), up to CPs
+    at the FP64 noise floor."""
+    ref = w12.autocritic(prec="fp64")
+    res = w12.autocritic(prec="tf32x3")
+    def unmatched(a, b):
+        out = []
+        for i, x in enumerate(a["xyz"]):
+            if np.min(np.linalg.norm(b["xyz"] - x, axis=1)) > 1e-6:
+                out.append(i)
+        return out
+    for i in unmatched(ref, res):
+        assert o12.grd(ref["xyz"][i], 2).gfmod < 1e-9
+    for i in unmatched(res, ref):
+        assert o12.grd(res["xyz"][i], 2).gfmod < 1e-9
+    assert len(unmatched(ref, res)) <= max(1, len(ref["xyz"]) // 50)
+    print(f"\nAUTO nci12: fp64 {ref['counts']} ph {ref['ph']} ({ref['ms']:.0f} ms), "
+          f"tf32x3 {res['counts']} ph {res['ph']} ({res['ms']:.0f} ms)")
