@@ -54,6 +54,14 @@ struct __align__(16) PrimTC {
   int pad[3];
 };
 
+// Stage primitive data as the producer warp keeps it in shared memory: three
+// 16-byte rows per primitive, read back as broadcast loads.
+struct __align__(16) StageRow {
+  float4 o;  // ox, oy, oz, g
+  float4 l;  // lx, ly, lz, t
+  float4 c;  // al2e, alpha, lp (bits), direct (bits)
+};
+
 struct TcKind {
   bool built = false;
   int kps = 0;        // primitives per K-stage
@@ -136,6 +144,7 @@ struct Smem {
   float4 *off;   // [2][natom] o = reference - atom: (o_hi, |o|^2_hi)
   float4 *offl;  // [2][natom] (o - o_hi, |o|^2 - |o|^2_hi)
   float *dmin;   // [2][natom] lower bound of the tile-atom distance
+  StageRow *rows;  // [NPROD][16] stage primitive data of each producer warp
 };
 
 __host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs) {
@@ -159,12 +168,13 @@ __host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs)
   offs[10] = take((size_t)2 * natom * 16, 16);
   offs[11] = take((size_t)2 * natom * 16, 16);
   offs[12] = take((size_t)2 * natom * 4, 16);
+  offs[13] = take((size_t)K::NPROD * 16 * sizeof(StageRow), 16);
   return o + 1024;  // slack for aligning the dynamic base
 }
 
 __device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
   uint8_t *base = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
-  size_t o[13];
+  size_t o[14];
   smem_bytes(natom, maskw, o);
   Smem s;
   s.stage = base + o[0];
@@ -184,6 +194,7 @@ __device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
   s.off = (float4 *)(base + o[10]);
   s.offl = (float4 *)(base + o[11]);
   s.dmin = (float *)(base + o[12]);
+  s.rows = (StageRow *)(base + o[13]);
   return s;
 }
 
@@ -213,7 +224,8 @@ __device__ __forceinline__ bool thread_wait(const Smem &s, int bar, uint32_t par
 
 // Factors of one Cartesian axis (see k_fp64.cu): with t = -2 alpha,
 //   f0 = x^l, f1 = l x^(l-1) + t x^(l+1), f2 = l(l-1) x^(l-2) + t(2l+1) x^l + t^2 x^(l+2)
-__device__ __forceinline__ void axis3(float x, int l, float t, float &f0, float &f1, float &f2) {
+// Generic form (any l), used for stages that hold g or h functions.
+__device__ __forceinline__ void axis_any(float x, int l, float t, float &f0, float &f1, float &f2) {
   float a = 1.f, b = 0.f, c = 0.f;
   for (int i = 0; i < l; i++) {
     c = b;
@@ -226,6 +238,21 @@ __device__ __forceinline__ void axis3(float x, int l, float t, float &f0, float 
   f2 = fmaf(t * t, p2, fmaf(t * (float)(2 * l + 1), a, (float)(l * (l - 1)) * c));
 }
 
+// Branch-free form for l <= 3 (s, p, d, f): x^l, x^(l-1), x^(l-2) are picked
+// from the powers of x by the bits of l, so that the factors of several
+// primitives can be evaluated as one straight-line block.
+__device__ __forceinline__ void axis_f(float x, int l, float t, float &f0, float &f1, float &f2) {
+  const float x2 = x * x;
+  const float a = ((l & 1) ? x : 1.f) * ((l & 2) ? x2 : 1.f);  // x^l
+  const int lm = l - 1;
+  const float b = l ? ((lm & 1) ? x : 1.f) * ((lm & 2) ? x2 : 1.f) : 0.f;  // x^(l-1)
+  const float c = (l >= 2) ? ((l == 3) ? x : 1.f) : 0.f;                   // x^(l-2)
+  const float fl = (float)l;
+  f0 = a;
+  f1 = fmaf(t * x, a, fl * b);
+  f2 = fmaf(a, fmaf(t * t, x2, t * (float)(2 * l + 1)), fl * (fl - 1.f) * c);
+}
+
 // Per (tile, primitive) part of the Gaussian.  With d = o + delta (o = tile
 // reference - atom, delta = point - reference):
 //   exp(-alpha |d|^2) = exp(-alpha |o|^2) * exp(-alpha (2 o.delta + |delta|^2)).
@@ -236,53 +263,90 @@ __device__ __forceinline__ void axis3(float x, int l, float t, float &f0, float 
 // turns critic2's cutoff d <= dran into 2 o.delta + |delta|^2 <= T.  When
 // alpha (2|o|R + R^2) is large (tight primitives; R = tile radius) the
 // per-point factor could overflow, and the primitive is evaluated directly
-// from the float-float distance instead (direct = true).
-struct PrimTile {
-  float g, t;
-  bool direct;
+// from the float-float distance instead (G = 1, exponent alpha |d|^2).
+struct StagePrim {
+  float ox, oy, oz, lx, ly, lz;  // o = hi + lo
+  float g, t, al2e, alpha;
+  int lp, direct;
 };
 
-__device__ __forceinline__ PrimTile prim_tile(const PrimTC &pr, const float4 &o, const float4 &ol, float rad) {
-  PrimTile r;
+__device__ __forceinline__ StagePrim stage_prim(const PrimTC &pr, const float4 &o, const float4 &ol, float rad) {
+  StagePrim q;
+  q.ox = o.x, q.oy = o.y, q.oz = o.z, q.lx = ol.x, q.ly = ol.y, q.lz = ol.z;
   const float ooh = o.w, ool = ol.w;
-  // arg = alpha * |o|^2 as hi + lo
   const float p = pr.alpha * ooh;
   float pe = fmaf(pr.alpha, ooh, -p);
   pe = fmaf(pr.alpha, ool, fmaf(pr.alpha_lo, ooh, pe));
-  // u = arg * log2(e), log2(e) = L1 + L2
   const float L1 = 1.44269502162933349609375f, L2 = 1.925963033500011079e-8f;
   const float u = p * L1;
   float ue = fmaf(p, L1, -u);
   ue = fmaf(p, L2, fmaf(pe, L1, ue));
   const float n = rintf(u);
   const float f = (u - n) + ue;
-  r.g = (n > 250.f) ? 0.f : ldexpf(exp2f(-f), -(int)n);
-  r.t = pr.dran * pr.dran - (ooh + ool);
   const float on = sqrtf(ooh);
-  r.direct = pr.alpha * (2.f * on * rad + rad * rad) > 60.f;
-  return r;
+  q.direct = pr.alpha * (2.f * on * rad + rad * rad) > 60.f;
+  q.g = q.direct ? 1.f : ((n > 250.f) ? 0.f : ldexpf(exp2f(-f), -(int)n));
+  // cutoff threshold on t (factorised) or on |d|^2 (direct); -inf for padding
+  q.t = pr.dran > 0.f ? (q.direct ? pr.dran * pr.dran : pr.dran * pr.dran - (ooh + ool)) : -INFINITY;
+  q.al2e = pr.al2e;
+  q.alpha = pr.alpha;
+  q.lp = pr.meta & 0xfff;
+  return q;
 }
 
+__device__ __forceinline__ StagePrim load_stage_prim(const StageRow *rows, int j) {
+  const float4 o = rows[j].o, l = rows[j].l, c = rows[j].c;
+  StagePrim q;
+  q.ox = o.x, q.oy = o.y, q.oz = o.z, q.g = o.w;
+  q.lx = l.x, q.ly = l.y, q.lz = l.z, q.t = l.w;
+  q.al2e = c.x, q.alpha = c.y, q.lp = __float_as_int(c.z), q.direct = __float_as_int(c.w);
+  return q;
+}
+
+__device__ __forceinline__ StagePrim bcast(const StagePrim &v, int j) {
+  StagePrim q;
+  q.ox = __shfl_sync(0xffffffffu, v.ox, j);
+  q.oy = __shfl_sync(0xffffffffu, v.oy, j);
+  q.oz = __shfl_sync(0xffffffffu, v.oz, j);
+  q.lx = __shfl_sync(0xffffffffu, v.lx, j);
+  q.ly = __shfl_sync(0xffffffffu, v.ly, j);
+  q.lz = __shfl_sync(0xffffffffu, v.lz, j);
+  q.g = __shfl_sync(0xffffffffu, v.g, j);
+  q.t = __shfl_sync(0xffffffffu, v.t, j);
+  q.al2e = __shfl_sync(0xffffffffu, v.al2e, j);
+  q.alpha = __shfl_sync(0xffffffffu, v.alpha, j);
+  q.lp = __shfl_sync(0xffffffffu, v.lp, j);
+  q.direct = __shfl_sync(0xffffffffu, v.direct, j);
+  return q;
+}
+
+// Point data: delta (offset from the tile reference), 2*delta, |delta|^2.
+struct PointD {
+  float x, y, z, x2, y2, z2, dd;
+  bool valid;
+};
+
 // chi (10 components) of one primitive at one point; zero beyond the cutoff
-__device__ __forceinline__ void chi10(const PrimTC &pr, const PrimTile &pt, const float4 &o, const float4 &ol,
-                                      const float4 &d, float dd, float (&chi)[10]) {
-  const float dx = (o.x + d.x) + ol.x, dy = (o.y + d.y) + ol.y, dz = (o.z + d.z) + ol.z;
-  float ex;
-  if (!pt.direct) {
-    const float t = fmaf(2.f * o.x, d.x, fmaf(2.f * o.y, d.y, fmaf(2.f * o.z, d.z, dd)));
-    const bool in = (d.w > 0.f) && (pr.dran > 0.f) && (t <= pt.t);
-    ex = in ? pt.g * exp2f(-pr.al2e * t) : 0.f;
-  } else {
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const bool in = (d.w > 0.f) && (pr.dran > 0.f) && (d2 <= pr.dran * pr.dran);
-    ex = in ? exp2f(-pr.al2e * d2) : 0.f;
-  }
-  const int lp = pr.meta;
-  const float tt = -2.f * pr.alpha;
+template <bool ANYL>
+__device__ __forceinline__ void chi10(const StagePrim &q, const PointD &d, float (&chi)[10]) {
+  const float dx = (q.ox + d.x) + q.lx, dy = (q.oy + d.y) + q.ly, dz = (q.oz + d.z) + q.lz;
+  const float t = fmaf(q.ox, d.x2, fmaf(q.oy, d.y2, fmaf(q.oz, d.z2, d.dd)));
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float targ = q.direct ? d2 : t;
+  const bool in = d.valid && (targ <= q.t);
+  const float e = exp2f(-q.al2e * targ);
+  const float ex = in ? q.g * e : 0.f;
+  const float tt = -2.f * q.alpha;
   float x0, x1, x2, y0, y1, y2, z0, z1, z2;
-  axis3(dx, lp & 15, tt, x0, x1, x2);
-  axis3(dy, (lp >> 4) & 15, tt, y0, y1, y2);
-  axis3(dz, (lp >> 8) & 15, tt, z0, z1, z2);
+  if constexpr (ANYL) {
+    axis_any(dx, q.lp & 15, tt, x0, x1, x2);
+    axis_any(dy, (q.lp >> 4) & 15, tt, y0, y1, y2);
+    axis_any(dz, (q.lp >> 8) & 15, tt, z0, z1, z2);
+  } else {
+    axis_f(dx, q.lp & 15, tt, x0, x1, x2);
+    axis_f(dy, (q.lp >> 4) & 15, tt, y0, y1, y2);
+    axis_f(dz, (q.lp >> 8) & 15, tt, z0, z1, z2);
+  }
   const float yz = y0 * z0 * ex, xz = x0 * z0 * ex, xy = x0 * y0 * ex;
   chi[0] = x0 * yz;
   chi[1] = x1 * yz;
@@ -303,89 +367,84 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
   return r;
 }
 
-// Builds one K-stage of the basis block: lane = point row, both 16-byte
-// halves of the 32-byte row, 10 components x (hi, lo) pieces, in the K-major
-// no-swizzle canonical layout (8-row core matrices of 16 bytes; the two
-// K-halves 128 bytes apart, 8-row groups 256 bytes apart).
-template <int KIND>
-__device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
-                                        const float4 &d, float dd, float rad) {
-  constexpr int KPS = KIND == 0 ? 16 : 8;
+// One 16-byte half of the 32-byte K-row of one point: PPB primitives,
+// 10 components x (hi, lo) pieces staged in registers, then stored with
+// 16-byte stores into the K-major no-swizzle canonical layout (8-row core
+// matrices of 16 bytes; the two K-halves 128 bytes apart, 8-row groups 256
+// bytes apart).
+template <int KIND, bool ANYL>
+__device__ __noinline__ void produce_half(const StageRow *rows, int half, const PointD &d, uint8_t *dst) {
   constexpr int PPB = KIND == 0 ? 8 : 4;  // primitives per 16-byte half row
   const int r = threadIdx.x & 31;
-  const float4 *off = s.off + par * a.w.natom;
-  const float4 *offl = s.offl + par * a.w.natom;
-  // per-(tile, primitive) Gaussian factors, lane j for primitive j
-  float pg = 0.f, ptt = 0.f;
-  int pdir = 0;
+  uint32_t wv[10][2][4];
+#pragma unroll
+  for (int j = 0; j < PPB; j += (KIND == 0 ? 2 : 1)) {
+    if constexpr (KIND == 0) {
+      float c0[10], c1[10];
+      chi10<ANYL>(load_stage_prim(rows, half * PPB + j), d, c0);
+      chi10<ANYL>(load_stage_prim(rows, half * PPB + j + 1), d, c1);
+#pragma unroll
+      for (int c = 0; c < 10; c++) {
+        const __nv_bfloat162 hi = __floats2bfloat162_rn(c0[c], c1[c]);
+        const float2 hf = __bfloat1622float2(hi);
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(c0[c] - hf.x, c1[c] - hf.y);
+        wv[c][0][j >> 1] = *reinterpret_cast<const uint32_t *>(&hi);
+        wv[c][1][j >> 1] = *reinterpret_cast<const uint32_t *>(&lo);
+      }
+    } else {
+      float c0[10];
+      chi10<ANYL>(load_stage_prim(rows, half * PPB + j), d, c0);
+#pragma unroll
+      for (int c = 0; c < 10; c++) {
+        const uint32_t hi = tf32_rna(c0[c]);
+        wv[c][0][j] = hi;
+        wv[c][1][j] = tf32_rna(c0[c] - __uint_as_float(hi));
+      }
+    }
+  }
+  uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
+#pragma unroll
+  for (int c = 0; c < 10; c++)
+#pragma unroll
+    for (int pc = 0; pc < 2; pc++)
+      *reinterpret_cast<uint4 *>(row + (c * 2 + pc) * K::PIECE) =
+          make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
+}
+
+// Builds one K-stage of the basis block (lane = point row).  The stage's
+// primitive data is loaded once (lane j holds primitive j) and broadcast.
+template <int KIND>
+__device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
+                                        const PointD &d, float rad, StageRow *rows) {
+  constexpr int KPS = KIND == 0 ? 16 : 8;
+  const int r = threadIdx.x & 31;
+  int lmax = 0;
   if (r < KPS) {
     const PrimTC pr = a.prim[stage_k + r];
     const int at = pr.meta >> 12;
-    const PrimTile q = prim_tile(pr, off[at], offl[at], rad);
-    pg = q.g;
-    ptt = q.t;
-    pdir = q.direct;
+    const StagePrim q = stage_prim(pr, s.off[par * a.w.natom + at], s.offl[par * a.w.natom + at], rad);
+    rows[r].o = make_float4(q.ox, q.oy, q.oz, q.g);
+    rows[r].l = make_float4(q.lx, q.ly, q.lz, q.t);
+    rows[r].c = make_float4(q.al2e, q.alpha, __int_as_float(q.lp), __int_as_float(q.direct));
+    lmax = max(q.lp & 15, max((q.lp >> 4) & 15, (q.lp >> 8) & 15));
   }
-#pragma unroll 1
+  lmax = __reduce_max_sync(0xffffffffu, lmax);  // also orders the row writes before the reads
   for (int half = 0; half < 2; half++) {
-    uint32_t wv[10][2][4];
-    const int k0 = stage_k + half * PPB;
-#pragma unroll
-    for (int j = 0; j < PPB; j += (KIND == 0 ? 2 : 1)) {
-#pragma unroll
-      for (int jj = 0; jj < (KIND == 0 ? 2 : 1); jj++) {
-        const int jl = half * PPB + j + jj;
-        const PrimTC pr = a.prim[k0 + j + jj];
-        const int at = pr.meta >> 12;
-        PrimTile q;
-        q.g = __shfl_sync(0xffffffffu, pg, jl);
-        q.t = __shfl_sync(0xffffffffu, ptt, jl);
-        q.direct = __shfl_sync(0xffffffffu, pdir, jl) != 0;
-        float c0[10];
-        chi10(pr, q, off[at], offl[at], d, dd, c0);
-        if constexpr (KIND == 0) {
-          // pairs of primitives share a 32-bit word (element k0+j in the low
-          // half): stash the first one's values, pack when the second is known
-          if (jj == 0) {
-#pragma unroll
-            for (int c = 0; c < 10; c++) wv[c][0][j >> 1] = __float_as_uint(c0[c]);
-          } else {
-#pragma unroll
-            for (int c = 0; c < 10; c++) {
-              const float c_lo = __uint_as_float(wv[c][0][j >> 1]);
-              const __nv_bfloat162 hi = __floats2bfloat162_rn(c_lo, c0[c]);
-              const float2 hf = __bfloat1622float2(hi);
-              const __nv_bfloat162 lo = __floats2bfloat162_rn(c_lo - hf.x, c0[c] - hf.y);
-              wv[c][0][j >> 1] = *reinterpret_cast<const uint32_t *>(&hi);
-              wv[c][1][j >> 1] = *reinterpret_cast<const uint32_t *>(&lo);
-            }
-          }
-        } else {
-#pragma unroll
-          for (int c = 0; c < 10; c++) {
-            const uint32_t hi = tf32_rna(c0[c]);
-            wv[c][0][j] = hi;
-            wv[c][1][j] = tf32_rna(c0[c] - __uint_as_float(hi));
-          }
-        }
-      }
-    }
-    uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
-#pragma unroll
-    for (int c = 0; c < 10; c++)
-#pragma unroll
-      for (int pc = 0; pc < 2; pc++)
-        *reinterpret_cast<uint4 *>(row + (c * 2 + pc) * K::PIECE) =
-            make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
+    if (lmax <= 3) produce_half<KIND, false>(rows, half, d, dst);
+    else produce_half<KIND, true>(rows, half, d, dst);
   }
+  __syncwarp();
 }
 
 // per-point outputs -----------------------------------------------------------
+// v[q*stride] are the point's 10 sums (rho, grad, hess xx yy zz xy xz yz),
+// FP32 when the molecule has one MO tile, FP64 accumulations otherwise.
 struct TcRecSink {
   double *rec;
-  __device__ void put(const TcArgs &, long idx, const double (&)[3], const double *acc) const {
+  template <class T>
+  __device__ void put(const TcArgs &, long idx, const T *v, int stride) const {
 #pragma unroll
-    for (int q = 0; q < 10; q++) rec[idx * 10 + q] = acc[q * 32];
+    for (int q = 0; q < 10; q++) rec[idx * 10 + q] = (double)v[q * stride];
   }
 };
 
@@ -424,29 +483,65 @@ __device__ void eig3_f64(double a00, double a11, double a22, double a01, double 
   ev[0] = e0; ev[1] = e1; ev[2] = e2;
 }
 
+// Same sweeps in FP32, for the points whose Hessian has a small eigenvalue.
+__device__ void eig3_f32(float a00, float a11, float a22, float a01, float a02, float a12, float (&ev)[3]) {
+  for (int sweep = 0; sweep < 8; sweep++) {
+    const float off = a01 * a01 + a02 * a02 + a12 * a12;
+    const float dia = a00 * a00 + a11 * a11 + a22 * a22;
+    if (off == 0.f || off < 1e-14f * dia) break;
+    if (a01 != 0.f) {
+      const float th = (a11 - a00) / (2.f * a01);
+      const float t = copysignf(1.f, th) / (fabsf(th) + sqrtf(th * th + 1.f));
+      const float c = rsqrtf(t * t + 1.f), s = t * c;
+      const float n02 = c * a02 - s * a12, n12 = s * a02 + c * a12;
+      a00 -= t * a01; a11 += t * a01; a01 = 0.f; a02 = n02; a12 = n12;
+    }
+    if (a02 != 0.f) {
+      const float th = (a22 - a00) / (2.f * a02);
+      const float t = copysignf(1.f, th) / (fabsf(th) + sqrtf(th * th + 1.f));
+      const float c = rsqrtf(t * t + 1.f), s = t * c;
+      const float n01 = c * a01 - s * a12, n12 = s * a01 + c * a12;
+      a00 -= t * a02; a22 += t * a02; a02 = 0.f; a01 = n01; a12 = n12;
+    }
+    if (a12 != 0.f) {
+      const float th = (a22 - a11) / (2.f * a12);
+      const float t = copysignf(1.f, th) / (fabsf(th) + sqrtf(th * th + 1.f));
+      const float c = rsqrtf(t * t + 1.f), s = t * c;
+      const float n01 = c * a01 - s * a02, n02 = s * a01 + c * a02;
+      a11 -= t * a12; a22 += t * a12; a12 = 0.f; a01 = n01; a02 = n02;
+    }
+  }
+  float e0 = a00, e1 = a11, e2 = a22, t;
+  if (e0 > e1) t = e0, e0 = e1, e1 = t;
+  if (e1 > e2) t = e1, e1 = e2, e2 = t;
+  if (e0 > e1) t = e0, e0 = e1, e1 = t;
+  ev[0] = e0; ev[1] = e1; ev[2] = e2;
+}
+
 // NCI point (src/nci@proc.f90:565-571, 598-599).  sign(lambda2) from the
 // characteristic polynomial (Descartes' rule is exact for the real roots of
 // a symmetric matrix) unless some eigenvalue is small relative to the
-// Hessian's scale; those points use an FP64 eigen-solve, and the ones with
-// |lambda2| < recheck_rel * max|lambda| go to the FP64 re-evaluation list.
-// rho^(4/3) is taken in FP64 where rho < 1e-4.
+// Hessian's scale; those points get an FP32 eigen-solve, and where
+// |lambda2| < 1e-3 max|lambda| the sign is decided by an FP64 eigen-solve;
+// the ones with |lambda2| < recheck_rel * max|lambda| go to the FP64
+// re-evaluation list.  rho^(4/3) is taken in FP64 where rho < 1e-4.
 struct TcNciSink {
   double *crho, *cgrad;
-  __device__ void put(const TcArgs &a, long idx, const double (&)[3], const double *acc) const {
-    const double rho = acc[0];
-    const float gx = (float)acc[32], gy = (float)acc[64], gz = (float)acc[96];
+  template <class T>
+  __device__ void put(const TcArgs &a, long idx, const T *v, int stride) const {
+    const float rf = (float)v[0];
+    const float gx = (float)v[stride], gy = (float)v[2 * stride], gz = (float)v[3 * stride];
     const float gm = sqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
     const float cst = 6.18733545256027186f;  // 2 (3 pi^2)^(1/3)
     double s;
-    if (rho >= 1e-4) {
-      const float r = (float)rho;
-      s = (double)(gm / (cst * r * cbrtf(r)));
+    if (rf >= 1e-4f) {
+      s = (double)(gm / (cst * rf * cbrtf(rf)));
     } else {
-      const double rr = fmax(rho, 1e-80);
+      const double rr = fmax((double)v[0], 1e-80);
       s = (double)gm / (6.18733545256027186 * rr * cbrt(rr));
     }
-    const float hxx = (float)acc[128], hyy = (float)acc[160], hzz = (float)acc[192];
-    const float hxy = (float)acc[224], hxz = (float)acc[256], hyz = (float)acc[288];
+    const float hxx = (float)v[4 * stride], hyy = (float)v[5 * stride], hzz = (float)v[6 * stride];
+    const float hxy = (float)v[7 * stride], hxz = (float)v[8 * stride], hyz = (float)v[9 * stride];
     const float tr = hxx + hyy + hzz;
     const float c2 = hxx * hyy - hxy * hxy + hxx * hzz - hxz * hxz + hyy * hzz - hyz * hyz;
     const float det = hxx * (hyy * hzz - hyz * hyz) - hxy * (hxy * hzz - hyz * hxz) + hxz * (hxy * hyz - hyy * hxz);
@@ -465,15 +560,23 @@ struct TcNciSink {
         }
       neg = changes < 2;
     } else {
-      double ev[3];
-      eig3_f64(acc[128], acc[160], acc[192], acc[224], acc[256], acc[288], ev);
-      neg = signbit(ev[1]);
-      const double big = fmax(fabs(ev[0]), fabs(ev[2]));
-      if (fabs(ev[1]) < (double)a.recheck_rel * big && a.recheck) {
-        const int slot = atomicAdd(a.recheck_count, 1);
-        if (slot < a.recheck_cap) a.recheck[slot] = (int)idx;
+      float ef[3];
+      eig3_f32(hxx, hyy, hzz, hxy, hxz, hyz, ef);
+      neg = signbit(ef[1]);
+      const float bigf = fmaxf(fabsf(ef[0]), fabsf(ef[2]));
+      if (fabsf(ef[1]) < fmaxf(2e-3f, 2.f * a.recheck_rel) * bigf) {
+        double ev[3];
+        eig3_f64((double)v[4 * stride], (double)v[5 * stride], (double)v[6 * stride], (double)v[7 * stride],
+                 (double)v[8 * stride], (double)v[9 * stride], ev);
+        neg = signbit(ev[1]);
+        const double big = fmax(fabs(ev[0]), fabs(ev[2]));
+        if (fabs(ev[1]) < (double)a.recheck_rel * big && a.recheck) {
+          const int slot = atomicAdd(a.recheck_count, 1);
+          if (slot < a.recheck_cap) a.recheck[slot] = (int)idx;
+        }
       }
     }
+    const double rho = (double)v[0];
     crho[idx] = (neg ? -fabs(rho) : fabs(rho)) * 100.0;
     cgrad[idx] = s;
   }
@@ -554,7 +657,7 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
         const float hx = (float)ox, hy = (float)oy, hz = (float)oz, ho = (float)oo;
         off[at] = make_float4(hx, hy, hz, ho);
         offl[at] = make_float4((float)(ox - hx), (float)(oy - hy), (float)(oz - hz), (float)(oo - ho));
-        dmn[at] = (float)sqrt(oo) - rad - 1e-3f;
+        dmn[at] = sqrtf(ho) - rad - 1e-3f;
       }
       if (lane == 0) s.rad[par] = rad;
       __syncwarp();
@@ -566,6 +669,7 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       uint8_t *key = s.key + par * a.maskw * 32;
       uint16_t *list = s.list + par * a.maskw * 32;
       constexpr int SPB = 32 / KPS;  // stages per ballot
+#pragma unroll 4
       for (int c0 = 0; c0 < a.maskw * 32; c0 += SPB) {
         const int k = c0 * KPS + lane;
         bool act = false;
@@ -662,8 +766,12 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
     for (int t = 0; t < ntl && ok; t++) {
       const int par = t & 1;
       if (!(ok = warp_wait(s, K::B_TREADY + par, (t >> 1) & 1, a.err))) break;
-      const float4 d = s.dl[par * 32 + lane];
-      const float dd = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+      const float4 d4 = s.dl[par * 32 + lane];
+      PointD d;
+      d.x = d4.x, d.y = d4.y, d.z = d4.z;
+      d.x2 = 2.f * d4.x, d.y2 = 2.f * d4.y, d.z2 = 2.f * d4.z;
+      d.dd = fmaf(d4.x, d4.x, fmaf(d4.y, d4.y, d4.z * d4.z));
+      d.valid = d4.w > 0.f;
       const float rad = s.rad[par];
       const uint16_t *list = s.list + par * a.maskw * 32;
       const int nact = s.nact[par];
@@ -674,7 +782,7 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           const int b = g % K::NSTAGE;
           if (g >= (uint32_t)K::NSTAGE && !(ok = warp_wait(s, K::B_EMPTY + b, ((g / K::NSTAGE) - 1) & 1, a.err)))
             break;
-          produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, dd, rad);
+          produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, rad, s.rows + pw * 16);
           ptx::fence_proxy_async_smem();
           __syncwarp();
           if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_CHI + b]);
@@ -778,21 +886,23 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
         if (q == 0) {
           if (!(ok = warp_wait(s, K::B_EPIFULL, u & 1, a.err))) break;
           const int p = lane;
+          float v4[10];
 #pragma unroll
           for (int k = 0; k < 10; k++) {
             const int i = (p >> 3) * 80 + k * 8 + (p & 7);
-            const float v4 = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
-            s.acc[k * 32 + p] += (double)v4;
+            v4[k] = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
           }
-          if (mt == a.nmt - 1) {
-            const long idx = s.idx[par * 32 + p];
-            if (idx >= 0) {
-              const double *sx = s.x + (par * 32 + p) * 3;
-              const double xx[3] = {sx[0], sx[1], sx[2]};
-              sink.put(a, idx, xx, s.acc + p);
-            }
+          const long idx = s.idx[par * 32 + p];
+          if (a.nmt == 1) {
+            if (idx >= 0) sink.put(a, idx, v4, 1);
+          } else {
 #pragma unroll
-            for (int k = 0; k < 10; k++) s.acc[k * 32 + p] = 0.0;
+            for (int k = 0; k < 10; k++) s.acc[k * 32 + p] += (double)v4[k];
+            if (mt == a.nmt - 1) {
+              if (idx >= 0) sink.put(a, idx, s.acc + p, 32);
+#pragma unroll
+              for (int k = 0; k < 10; k++) s.acc[k * 32 + p] = 0.0;
+            }
           }
           __syncwarp();
           if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_EPIFREE]);
@@ -960,7 +1070,7 @@ int sm_count() {
 template <int KIND, class Src, class Sink>
 void launch_tc(const TcArgs &a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st) {
   if (ntiles <= 0) return;
-  size_t offs[13];
+  size_t offs[14];
   const size_t bytes = smem_bytes(a.w.natom, a.maskw, offs);
   if (bytes > 227 * 1024) fail(C2G_ERR_UNSUPPORTED, "molecule too large for the split-precision kernel's shared memory");
   auto fn = k_tc<KIND, Src, Sink>;

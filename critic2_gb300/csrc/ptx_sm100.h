@@ -51,7 +51,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t timeout_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
+  uint32_t spins = 0;
   while (!mbar_try_wait(bar, parity)) {
+    // back off so that waiting warps leave the issue slots to working ones
+    if (++spins > 4) __nanosleep(spins < 64 ? 32u : 256u);
     if (globaltimer() - t0 > timeout_ns) return false;
   }
   return true;

@@ -93,7 +93,8 @@ int c2g_wfn_destroy(c2g_wfn *h);
 /* Tunable parameters of a handle. */
 #define C2G_PARAM_RECHECK_REL 1 /* split-precision NCI: points with
                                    |lambda2| < value * max|lambda| are
-                                   re-evaluated in FP64 (default 1e-3) */
+                                   re-evaluated in FP64 (default 1e-3;
+                                   values above 1e-3 act as 1e-3) */
 int c2g_wfn_set_param(c2g_wfn *h, int param, double value);
 
 /* Sizes after pruning. */
