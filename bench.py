@@ -167,8 +167,12 @@ def main():
     ap.add_argument("--prec", default="auto")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--grid", type=int, default=0, help="grid points per axis (default: the workload's)")
     args = ap.parse_args()
     wl = synth.WORKLOADS[args.workload]
+    if args.grid > 0:
+        import dataclasses
+        wl = dataclasses.replace(wl, grid=args.grid)
     mol = synth.make_molecule(args.workload)
     if args.impl == "reference":
         return run_reference(args, wl, mol)
@@ -205,9 +209,14 @@ def main():
     def step(stats=False):
         return w.nciplot_dev(x0, xm, ns, prec, crho.data_ptr(), cgrad.data_ptr(), sp, stats=stats)
 
-    for _ in range(args.warmup):
+    # W warm-up steps, extended (untimed) to at least ~1.5 s of GPU work so
+    # that the clocks have left their idle state before the timed region
+    t_w = time.perf_counter()
+    nw = 0
+    while nw < args.warmup or (time.perf_counter() - t_w < 1.5 and nw < args.warmup + 20):
         step()
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        nw += 1
     # device-resident timed region
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]

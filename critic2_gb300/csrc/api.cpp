@@ -363,8 +363,8 @@ int c2g_wfn_set_param(c2g_wfn *hp, int param, double value) {
   return guarded([&] {
     Handle *h = check_handle(hp);
     if (param == C2G_PARAM_RECHECK_REL) {
-      require(value >= 0.0 && value < 1.0, "re-check threshold must be in [0, 1)");
-      tc_set_recheck(*h, value);
+      require(value < 1.0, "re-check threshold must be below 1 (negative: the default)");
+      tc_set_recheck(*h, value < 0.0 ? -1.0 : value);
     } else {
       fail(C2G_ERR_ARG, "unknown parameter");
     }

@@ -78,7 +78,7 @@ struct TcOperands {
   int *err = nullptr;  // device error word
   std::vector<int> order;  // TC primitive order (indices into the handle's prims)
   std::vector<void *> allocs;
-  double recheck_rel = 1e-3;
+  double recheck_rel = -1.0;  // < 0: the mode's default (TF32x3 1e-4, BF16x3 1e-3)
   int *scratch = nullptr;  // re-check list + counter, grown on demand
   size_t scratch_cap = 0;  // ints
 };
@@ -1055,7 +1055,9 @@ TcArgs make_args(Handle &h, int kind) {
   a.recheck = nullptr;
   a.recheck_count = nullptr;
   a.recheck_cap = 0;
-  a.recheck_rel = (float)t->recheck_rel;
+  // Split Hessians carry ~1e-6 (TF32x3) / ~2e-5 (BF16x3) relative error, so
+  // sign(lambda2) can only be wrong well below these thresholds.
+  a.recheck_rel = (float)(t->recheck_rel >= 0.0 ? t->recheck_rel : (kind == 1 ? 1e-4 : 1e-3));
   a.stage_count = nullptr;
   return a;
 }

@@ -74,7 +74,8 @@ class Wavefunction:
 
     def set_recheck(self, rel: float):
         """Relative |lambda2| below which split-precision NCI points are
-        re-evaluated in FP64 (C2G_PARAM_RECHECK_REL)."""
+        re-evaluated in FP64 (C2G_PARAM_RECHECK_REL); negative restores the
+        mode's default (TF32x3 1e-4, BF16x3 1e-3), 0 disables it."""
         L.check(L.lib().c2g_wfn_set_param(self._h, 1, float(rel)))
 
     # ------------------------------------------------------------ rho2/grd

@@ -93,8 +93,10 @@ int c2g_wfn_destroy(c2g_wfn *h);
 /* Tunable parameters of a handle. */
 #define C2G_PARAM_RECHECK_REL 1 /* split-precision NCI: points with
                                    |lambda2| < value * max|lambda| are
-                                   re-evaluated in FP64 (default 1e-3;
-                                   values above 1e-3 act as 1e-3) */
+                                   re-evaluated in FP64.  Default (or any
+                                   negative value): 1e-4 for TF32X3, 1e-3
+                                   for BF16X3; 0 disables the re-check;
+                                   values above 1e-3 act as 1e-3 */
 int c2g_wfn_set_param(c2g_wfn *h, int param, double value);
 
 /* Sizes after pruning. */
@@ -152,7 +154,8 @@ int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int 
 /* field%newton for n seeds at once (src/fieldmod@proc.f90:2238-2279):
  * xyz(3,n) in/out; ier(n): 0 converged (|grad| < gfnormeps), 1 invalid or
  * singular Hessian, 2 maxit reached.  In the split modes the iterations run
- * in split precision until |grad| < 1e-5 and finish in FP64. */
+ * in split precision until the Newton step is shorter than 1e-5 bohr and
+ * finish in FP64 (convergence is only declared from an FP64 evaluation). */
 int c2g_newton(c2g_wfn *h, int n, double *xyz, double gfnormeps, int maxit, int prec, int *ier);
 
 /* Default molecular pair seeds of critic2's AUTO (src/autocp@proc.f90:

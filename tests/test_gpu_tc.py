@@ -127,8 +127,10 @@ def test_recheck_threshold(w12, mol12):
     c0, _, st0 = w12.nciplot(x0, xm, ns, "tf32x3")
     w12.set_recheck(0.5)
     c1, _, st1 = w12.nciplot(x0, xm, ns, "tf32x3")
-    w12.set_recheck(1e-3)
+    w12.set_recheck(-1.0)
+    _, _, std = w12.nciplot(x0, xm, ns, "tf32x3")
     assert st0.nrecheck == 0 and st1.nrecheck > 0
+    assert st1.nrecheck >= std.nrecheck
     # re-checked points are the FP64 values exactly
     assert np.sum(np.sign(c1) != np.sign(c64)) <= np.sum(np.sign(c0) != np.sign(c64))
 
