@@ -20,7 +20,8 @@ ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported"}
 # every symbol include/critic2_gb300.h declares
 EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx",
            "c2g_wfn_destroy", "c2g_wfn_set_param", "c2g_wfn_info", "c2g_rho2", "c2g_grd", "c2g_nciplot",
-           "c2g_nciplot_dev", "c2g_newton", "c2g_pair_seeds", "c2g_autocritic")
+           "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
+           "c2g_autocritic")
 
 
 class C2GError(RuntimeError):
@@ -66,6 +67,7 @@ def lib():
     L.c2g_grd.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int] + [_vp] * 8
     L.c2g_nciplot.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, C.POINTER(NciStats)]
     L.c2g_nciplot_dev.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, _vp, C.POINTER(NciStats)]
+    L.c2g_nciplot_dev_noalloc.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, _vp]
     L.c2g_newton.argtypes = [_vp, C.c_int, _vp, C.c_double, C.c_int, C.c_int, _vp]
     L.c2g_pair_seeds.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(C.c_int)]
     L.c2g_autocritic.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int, _vp, _vp, _vp,

@@ -498,6 +498,31 @@ int c2g_nciplot_dev(c2g_wfn *hp, const double *x0, const double *xmat, const int
   });
 }
 
+int c2g_nciplot_dev_noalloc(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec,
+                            double *d_crho, double *d_cgrad, void *stream) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(x0 && xmat && nstep && d_crho && d_cgrad, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    const long np = (long)nstep[0] * nstep[1] * nstep[2];
+    if (np > tc_noalloc_max_points())
+      fail(C2G_ERR_ARG, "grid has " + std::to_string(np) + " points; the no-allocation entry takes at most " +
+                            std::to_string(tc_noalloc_max_points()) + " per call (split the grid into slabs)");
+    check_prec(prec);
+    DeviceGuard g(h->device);
+    GridSpec gs;
+    for (int j = 0; j < 3; j++) gs.x0[j] = x0[j], gs.nstep[j] = nstep[j];
+    for (int j = 0; j < 9; j++) gs.xmat[j] = xmat[j];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (prec == C2G_PREC_FP64) {
+      launch_fp64_nci_grid(h->dev, gs, d_crho, d_cgrad, st);  // uses no scratch
+      C2G_CUDA(cudaStreamSynchronize(st));
+    } else {
+      tc_nci_grid_noalloc(*h, prec, gs, d_crho, d_cgrad, st);
+    }
+  });
+}
+
 int c2g_nciplot(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec,
                 double *crho, double *cgrad, c2g_nci_stats *stats) {
   return guarded([&] {

@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -113,6 +114,10 @@ constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17,
               B_EPIFREE = 19, B_TREADY = 20, B_TFREE = 22, B_DRAIN = 24, NBAR = 25;
 static_assert(NSTAGE == NPROD, "one producer warp per stage buffer");
 }  // namespace K
+
+struct Mat3 {
+  double m[9];
+};
 
 struct TcArgs {
   DevWfn w;
@@ -925,6 +930,37 @@ __global__ void k_zero_cgrad(double *cgrad, const int *idx, int n) {
   if (i < n) cgrad[idx[i]] = 0.0;
 }
 
+// Scratch of the no-allocation NCI entry: the FP64 re-check list (one slot
+// per grid point, kNoAllocMaxPoints points at most) followed by its
+// counter.  Lives in the module's static device memory, so the entry needs
+// no allocation at call time; it is shared by every call on the device.
+constexpr int kNoAllocMaxPoints = 1 << 20;
+constexpr int kNoAllocTail = 64;  // counter + padding (256 bytes)
+static __device__ __align__(256) int g_noalloc_scratch[kNoAllocMaxPoints + kNoAllocTail];
+
+// Nucleus rule on a split-precision grid, located on the device: grid
+// points within 1e-5 bohr of a nucleus get s = 0 (src/fieldmod@proc.f90:
+// 1148-1154).  inv is the inverse of xmat (column-major).
+__global__ void k_nucleus_cgrad(const double4 *atoms, int natom, GridSpec g, Mat3 inv, double *cgrad) {
+  const int at = blockIdx.x * blockDim.x + threadIdx.x;
+  if (at >= natom) return;
+  const double4 A = atoms[at];
+  const double r[3] = {A.x - g.x0[0], A.y - g.x0[1], A.z - g.x0[2]};
+  long ii[3];
+  for (int c = 0; c < 3; c++) {
+    const double f = inv.m[c] * r[0] + inv.m[3 + c] * r[1] + inv.m[6 + c] * r[2];
+    ii[c] = llrint(f);
+    if (ii[c] < 0 || ii[c] >= g.nstep[c]) return;
+  }
+  double d2 = 0.0;
+  const double xyz[3] = {A.x, A.y, A.z};
+  for (int c = 0; c < 3; c++) {
+    const double x = g.x0[c] + ii[0] * g.xmat[c] + ii[1] * g.xmat[3 + c] + ii[2] * g.xmat[6 + c];
+    d2 += (x - xyz[c]) * (x - xyz[c]);
+  }
+  if (sqrt(d2) <= 1e-5) cgrad[(ii[0] * g.nstep[1] + ii[1]) * g.nstep[2] + ii[2]] = 0.0;
+}
+
 // ------------------------------------------------------------------- host
 uint32_t morton3(const double *p, const double *lo, const double *span) {
   uint32_t q[3];
@@ -1250,6 +1286,76 @@ long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double 
   check_device_error(h.tc);
   if (stage_frac) *stage_frac = (double)hstages / ((double)ntiles * t->kind[kind].nstage);
   return hcount;
+}
+
+long tc_noalloc_max_points() { return kNoAllocMaxPoints; }
+
+void tc_nci_grid_noalloc(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad, cudaStream_t st) {
+  const int kind = kind_of(prec);
+  TcOperands *t = h.tc;
+  if (!t->kind[kind].built)
+    fail(C2G_ERR_UNSUPPORTED,
+         "the split operands of this precision mode are not on the device yet; they are allocated by the first "
+         "split-precision call of an allocating entry (e.g. c2g_nciplot_dev on a 1-point grid)");
+  const long npts = (long)g.nstep[0] * g.nstep[1] * g.nstep[2];
+  if (npts > kNoAllocMaxPoints)
+    fail(C2G_ERR_ARG, "grid has " + std::to_string(npts) + " points; the no-allocation entry takes at most " +
+                          std::to_string(kNoAllocMaxPoints) + " per call (split the grid into slabs)");
+  // once per device, with that device current: the address of the scratch
+  static std::mutex mu;
+  static int *ptr_of[64] = {nullptr};
+  int dev = 0;
+  C2G_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) fail(C2G_ERR_UNSUPPORTED, "device ordinal above 63");
+  int *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!ptr_of[dev]) {
+      void *p = nullptr;
+      const cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (rc != cudaSuccess) fail(C2G_ERR_CUDA, std::string("cudaGetSymbolAddress (no-allocation scratch): ") +
+                                                    cudaGetErrorString(rc));
+      ptr_of[dev] = static_cast<int *>(p);
+    }
+    scratch = ptr_of[dev];
+  }
+  int *count = scratch + kNoAllocMaxPoints;
+  // the re-check counter must start at zero
+  C2G_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
+  TcArgs a = make_args(h, kind);
+  a.recheck = scratch;
+  a.recheck_count = count;
+  a.recheck_cap = (int)npts;
+  GridSrc src{g, (g.nstep[1] + 3) / 4, (g.nstep[2] + 7) / 8};
+  const long ntiles = (long)g.nstep[0] * src.ntj * src.ntk;
+  launch_kind(kind, a, src, TcNciSink{d_crho, d_cgrad}, (int)ntiles, st);
+  launch_fp64_nci_list(h.dev, g, scratch, count, (int)npts, d_crho, d_cgrad, st);
+  const double *M = g.xmat;
+  const double det = M[0] * (M[4] * M[8] - M[7] * M[5]) - M[3] * (M[1] * M[8] - M[7] * M[2]) +
+                     M[6] * (M[1] * M[5] - M[4] * M[2]);
+  if (det != 0.0 && h.dev.natom > 0) {
+    Mat3 inv;
+    inv.m[0] = (M[4] * M[8] - M[5] * M[7]) / det;
+    inv.m[3] = (M[5] * M[6] - M[3] * M[8]) / det;
+    inv.m[6] = (M[3] * M[7] - M[4] * M[6]) / det;
+    inv.m[1] = (M[2] * M[7] - M[1] * M[8]) / det;
+    inv.m[4] = (M[0] * M[8] - M[2] * M[6]) / det;
+    inv.m[7] = (M[1] * M[6] - M[0] * M[7]) / det;
+    inv.m[2] = (M[1] * M[5] - M[2] * M[4]) / det;
+    inv.m[5] = (M[2] * M[3] - M[0] * M[5]) / det;
+    inv.m[8] = (M[0] * M[4] - M[1] * M[3]) / det;
+    k_nucleus_cgrad<<<(h.dev.natom + 127) / 128, 128, 0, st>>>(h.dev.atoms, h.dev.natom, g, inv, d_cgrad);
+    C2G_CUDA(cudaGetLastError());
+  }
+  // pipeline timeouts of the split kernel are reported by this call
+  int e = 0;
+  C2G_CUDA(cudaMemcpyAsync(&e, t->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  C2G_CUDA(cudaStreamSynchronize(st));
+  if (e) {
+    C2G_CUDA(cudaMemsetAsync(t->err, 0, sizeof(int), st));
+    C2G_CUDA(cudaStreamSynchronize(st));
+    fail(C2G_ERR_CUDA, "split-precision kernel: a pipeline wait timed out (mask " + std::to_string(e) + ")");
+  }
 }
 
 }  // namespace c2g

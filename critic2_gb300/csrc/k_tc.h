@@ -25,10 +25,19 @@ void tc_points_index(Handle &h, int prec, const double *d_x, const int *d_idx, c
                      int maxn, double *d_rec, cudaStream_t st);
 
 // NCI grid in split precision followed by the FP64 re-check of the points
-// whose Hessian has |lambda2| < 1e-3 |lambda1|.  Records ev_split after the
+// whose Hessian has a small |lambda2| relative to max|lambda| (threshold:
+// C2G_PARAM_RECHECK_REL).  Records ev_split after the
 // split pass when not null, and the fraction of active K-stages per tile in
 // *stage_frac when not null.  Returns the number of re-checked points.
 long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad,
                  cudaStream_t st, cudaEvent_t ev_split, double *stage_frac);
+
+// No-allocation variant of tc_nci_grid: the re-check list lives in static
+// device memory (at most tc_noalloc_max_points() grid points per call), the
+// nucleus rule runs on the device; no statistics.  Fails when the handle's
+// split operands for prec were not built yet.
+void tc_nci_grid_noalloc(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad,
+                         cudaStream_t st);
+long tc_noalloc_max_points();
 
 }  // namespace c2g

@@ -130,6 +130,16 @@ class Wavefunction:
                                         C.c_void_p(stream), C.byref(st) if stats else None))
         return st
 
+    def nciplot_dev_noalloc(self, x0, xmat, nstep, prec, d_crho: int, d_cgrad: int, stream: int = 0):
+        """NCI grid into device buffers without any device allocation by the
+        library (c2g_nciplot_dev_noalloc: at most 2^20 points per call, split
+        operands of `prec` built by an earlier call, calls on one device
+        serialised by the caller)."""
+        xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+        L.check(L.lib().c2g_nciplot_dev_noalloc(self._h, _f64(x0), xm, _i32(nstep), _prec(prec),
+                                                C.c_void_p(d_crho), C.c_void_p(d_cgrad),
+                                                C.c_void_p(stream)))
+
     # -------------------------------------------------------------- Newton
     def newton(self, xyz, gfnormeps: float = 1e-12, maxit: int = 200, prec="fp64"):
         x = _f64(xyz).reshape(-1, 3).copy()

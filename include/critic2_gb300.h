@@ -151,6 +151,36 @@ int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int 
                     int prec, double *d_crho, double *d_cgrad, void *stream,
                     c2g_nci_stats *stats);
 
+/* No-allocation form of c2g_nciplot_dev (this entry has no counterpart in
+ * the reference).  For callers that cannot let the library allocate device
+ * memory during a run: codes whose memory is reserved up front by their own
+ * pool (a caching allocator that holds the GPU's memory, or an MPI job that
+ * sizes everything at start-up) and codes that stream grid slabs on their
+ * own streams, where cudaFree -- which synchronises the whole device --
+ * would stall their other work.  c2g_nciplot_dev allocates its FP64
+ * re-check list and a nucleus list; this entry keeps the re-check list in a
+ * static device array of 4 MiB + 256 B and applies the nucleus rule on the
+ * device, and makes no cudaMalloc/cudaFree or allocating-library call.
+ *   - At most C2G_NOALLOC_MAX_POINTS grid points per call; larger grids are
+ *     rejected with C2G_ERR_ARG (split them into i-slabs and call per slab).
+ *   - The split operands of the requested mode must already be on the
+ *     device: they are allocated by the first split-precision call of an
+ *     allocating entry (e.g. c2g_nciplot_dev on a 1-point grid); otherwise
+ *     the call returns C2G_ERR_UNSUPPORTED.  C2G_PREC_FP64 needs nothing.
+ *   - The first call on each device looks up the scratch array's address
+ *     (cudaGetSymbolAddress, with that device current); make that first
+ *     call before any stream capture.
+ *   - The re-check counter, which must start at zero, is cleared by the call
+ *     itself on the given stream.
+ *   - The scratch is shared by all calls on a device: calls that overlap in
+ *     time (other host threads, or other streams, on the same device) race
+ *     on it and must be serialised by the caller.
+ *   - Returns after the work on `stream` has finished (a pipeline timeout of
+ *     the split kernel is reported as C2G_ERR_CUDA).  No statistics. */
+#define C2G_NOALLOC_MAX_POINTS 1048576
+int c2g_nciplot_dev_noalloc(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep,
+                            int prec, double *d_crho, double *d_cgrad, void *stream);
+
 /* field%newton for n seeds at once (src/fieldmod@proc.f90:2238-2279):
  * xyz(3,n) in/out; ier(n): 0 converged (|grad| < gfnormeps), 1 invalid or
  * singular Hessian, 2 maxit reached.  In the split modes the iterations run
