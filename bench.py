@@ -38,6 +38,11 @@ from critic2_gb300 import synth  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
+# DRAM bytes (read + write) per grid point of the split evaluator, from one
+# ncu capture of k_tc on the nci60 molecule with a 64^3 grid (1.18 MB per
+# 262,144 points; traffic grows with the points, the operands stay in L2).
+TRAFFIC_PER_POINT = {("nci60", "tf32x3"): (1.163776e6 + 18688.0) / 262144}
+
 
 def env_int(k, d):
     try:
@@ -290,7 +295,9 @@ def main():
                     "d2h_bytes_per_step": 2 * 8 * npts},
             "gpu_launches": args.steps * (1 if prec == "fp64" else (3 if nrecheck else 2)),
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": (TRAFFIC_PER_POINT[(args.workload, prec)] * npts
+                                     if (args.workload, prec) in TRAFFIC_PER_POINT else None),
                          "note": f"algorithmic 20*nmo*npri flops per point over the evaluation "
                                  f"kernel time; peak = bf16 dense burst ({pk_kind})"},
             "fp64_recheck_points": nrecheck}
