@@ -21,7 +21,10 @@ ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported"}
 EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx",
            "c2g_wfn_destroy", "c2g_wfn_set_param", "c2g_wfn_info", "c2g_rho2", "c2g_grd", "c2g_nciplot",
            "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
-           "c2g_autocritic")
+           "c2g_autocritic",
+           # learned CP-seed proposer (include/critic2_gb300_cpseed.h)
+           "c2g_cs_conv3d", "c2g_cs_conv3d_bwd_data", "c2g_cs_conv3d_bwd_weight", "c2g_cs_loss",
+           "c2g_cs_targets", "c2g_cs_features", "c2g_cs_seeds", "c2g_cs_adam")
 
 
 class C2GError(RuntimeError):
@@ -72,6 +75,15 @@ def lib():
     L.c2g_pair_seeds.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(C.c_int)]
     L.c2g_autocritic.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int, _vp, _vp, _vp,
                                  C.POINTER(CpReport)]
+    i, f, lg = C.c_int, C.c_float, C.c_long
+    L.c2g_cs_conv3d.argtypes = [_vp, i, i, i, i, i, _vp, _vp, i, i, i, _vp, _vp]
+    L.c2g_cs_conv3d_bwd_data.argtypes = [_vp, i, i, i, i, i, _vp, i, i, _vp, _vp, _vp]
+    L.c2g_cs_conv3d_bwd_weight.argtypes = [_vp, _vp, i, i, i, i, i, i, i, _vp, _vp, _vp]
+    L.c2g_cs_loss.argtypes = [_vp, _vp, lg, i, f, f, _vp, _vp, _vp]
+    L.c2g_cs_targets.argtypes = [_vp, i, i, _vp, _vp]
+    L.c2g_cs_features.argtypes = [_vp, _vp, lg, _vp, _vp]
+    L.c2g_cs_seeds.argtypes = [_vp, i, _dp, C.c_double, f, i, i, _vp, _vp, _vp, _vp]
+    L.c2g_cs_adam.argtypes = [_vp, _vp, _vp, _vp, i, f, f, f, f, i, _vp]
     _lib = L
     return L
 

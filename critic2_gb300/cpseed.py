@@ -1,0 +1,424 @@
+"""Learned critical-point seeds for the AUTO search.
+
+critic2's AUTO seeds Newton from geometric guesses: for molecules, five
+points on every pair of atoms closer than 15 bohr (src/autocp@proc.f90:
+423-437), which for 100 atoms is tens of thousands of Newton runs.  Here a
+small 3D convolutional network reads a coarse grid of the density and
+proposes a few seeds per critical point; the seeds go through the unchanged
+Newton + addcp stages (`Wavefunction.autocritic(seeds)`), so every CP it
+reports is confirmed by exact-field (FP64-finished) Newton convergence and
+addcp's gradient check.  The result is accepted only if the CP list
+satisfies the Poincare-Hopf sum n - b + r - c = 1; otherwise the search is
+repeated with a denser seed set and, if that fails too, with critic2's
+plain pair seeds (the fallback).
+
+Pieces (all GPU work goes through the library's kernels; torch only holds
+device memory and streams):
+  coarse_grid / features  the S^3 grid (spacing h, centred on the molecule)
+                          evaluated by the NCI kernel (c2g_nciplot_dev),
+                          turned into 4 input channels (c2g_cs_features);
+  SeedNet                 5 convolutions 4-16-32-32-32 (3^3, ReLU) and a
+                          1^3 head to 8 channels (4 CP-type heat-map logits,
+                          3 sub-voxel offsets); forward, backward and Adam
+                          are the library's c2g_cs_* kernels; weights are
+                          stored and run as BF16 values;
+  cp_labels               training targets from a plain AUTO CP list;
+  propose / learned_autocritic  seeds and the confirmed search with the
+                          Poincare-Hopf check and fallback;
+  train (python -m critic2_gb300.cpseed train)  data generation with plain
+                          AUTO on seeded molecules and training on the GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import sys
+import time
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib as L
+from . import synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WEIGHTS = os.path.join(HERE, "cpseed_weights.npz")
+
+# (cin, cout, ksize, relu)
+LAYERS = ((4, 16, 3, True), (16, 32, 3, True), (32, 32, 3, True), (32, 32, 3, True), (32, 8, 1, False))
+TYPE_OF_SIGNATURE = {-3: 0, -1: 1, 1: 2, 3: 3}  # non-nuclear maximum, bond, ring, cage
+S_DEFAULT, H_DEFAULT = 64, 0.45
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _vp(t) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr())
+
+
+def bf16_round(a: np.ndarray) -> np.ndarray:
+    """Rounds FP32 values to the nearest BF16 value (ties to even)."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+# ------------------------------------------------------------------ grid
+def coarse_grid(atom_xyz: np.ndarray, S: int = S_DEFAULT, h: float = H_DEFAULT):
+    """S^3 grid of spacing h centred on the molecule's bounding box: returns
+    x0 (voxel (0,0,0)), xmat (diag h) and nstep."""
+    c = 0.5 * (atom_xyz.min(0) + atom_xyz.max(0))
+    x0 = c - 0.5 * h * (S - 1)
+    return x0.astype(np.float64), np.diag([h, h, h]).astype(np.float64), np.array([S, S, S], np.int32)
+
+
+def features(wfn, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: str = "tf32x3", out=None, stream=0):
+    """Network input for one molecule, on the GPU: the NCI kernel on the
+    coarse grid, then the feature kernel.  Returns (x [S^3*4] float32, x0)."""
+    torch = _torch()
+    x0, xm, ns = coarse_grid(_atoms(wfn), S, h)
+    n = S ** 3
+    crho = torch.empty(n, dtype=torch.float64, device="cuda")
+    cgrad = torch.empty(n, dtype=torch.float64, device="cuda")
+    wfn.nciplot_dev(x0, xm, ns, prec, crho.data_ptr(), cgrad.data_ptr(), stream)
+    x = out if out is not None else torch.empty(n * 4, dtype=torch.float32, device="cuda")
+    L.check(L.lib().c2g_cs_features(_vp(crho), _vp(cgrad), n, _vp(x), C.c_void_p(stream)))
+    return x, x0
+
+
+def _atoms(wfn) -> np.ndarray:
+    a = getattr(wfn, "atom_xyz", None)
+    if a is None:
+        raise ValueError("the wavefunction needs its atom coordinates (Wavefunction(mol) keeps them)")
+    return a
+
+
+def cp_labels(xyz: np.ndarray, typ: np.ndarray, atom_xyz: np.ndarray, x0: np.ndarray, h: float,
+              S: int, nuc_tol: float = 0.05) -> np.ndarray:
+    """Training targets from a CP list: rows (fi, fj, fk, type) for every
+    non-nuclear CP inside the grid, in fractional voxel coordinates; nuclei
+    (CPs of signature -3 within nuc_tol of an atom) are not learned, AUTO
+    adds them itself."""
+    rows = []
+    for x, t in zip(np.asarray(xyz).reshape(-1, 3), np.asarray(typ)):
+        t = int(t)
+        if t not in TYPE_OF_SIGNATURE:
+            continue
+        if t == -3 and np.min(np.linalg.norm(atom_xyz - x, axis=1)) < nuc_tol:
+            continue
+        f = (x - x0) / h
+        if np.all(f >= 0) and np.all(f <= S - 1):
+            rows.append((f[0], f[1], f[2], TYPE_OF_SIGNATURE[t]))
+    return np.array(rows, np.float32).reshape(-1, 4)
+
+
+# --------------------------------------------------------------- network
+class SeedNet:
+    """The proposer network on the GPU.  `params` and `grad` are flat FP32
+    device buffers; layer l's weights w[tap][cin][cout] and bias[cout]
+    are views into them."""
+
+    def __init__(self, seed: int = 0, params: Optional[np.ndarray] = None):
+        torch = _torch()
+        self.sizes = []
+        for cin, cout, k, _ in LAYERS:
+            self.sizes += [k ** 3 * cin * cout, cout]
+        self.n = int(sum(self.sizes))
+        if params is None:
+            rng = np.random.default_rng(seed)
+            parts = []
+            for (cin, cout, k, relu) in LAYERS:
+                std = np.sqrt(2.0 / (k ** 3 * cin)) if relu else np.sqrt(1.0 / (k ** 3 * cin))
+                parts.append(rng.standard_normal(k ** 3 * cin * cout) * std)
+                b = np.zeros(cout)
+                if not relu:
+                    b[:4] = -4.0  # heat maps start near p = 0.02
+                parts.append(b)
+            params = np.concatenate(parts)
+        assert params.size == self.n
+        self.params = torch.tensor(np.asarray(params, np.float32), device="cuda")
+        self.grad = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.t = 0
+        self._acts = None
+
+    def _views(self, buf):
+        out, o = [], 0
+        for i in range(0, len(self.sizes), 2):
+            w = buf[o:o + self.sizes[i]]
+            o += self.sizes[i]
+            b = buf[o:o + self.sizes[i + 1]]
+            o += self.sizes[i + 1]
+            out.append((w, b))
+        return out
+
+    def forward(self, x, B: int, S: int, keep: bool = False, stream: int = 0):
+        """x: [B*S^3*4] float32 on the GPU -> logits [B*S^3*8]."""
+        torch = _torch()
+        lib = L.lib()
+        n = B * S ** 3
+        acts = [x]
+        cur = x
+        for (cin, cout, k, relu), (w, b) in zip(LAYERS, self._views(self.params)):
+            y = torch.empty(n * cout, dtype=torch.float32, device="cuda")
+            L.check(lib.c2g_cs_conv3d(_vp(cur), B, S, S, S, cin, _vp(w), _vp(b), cout, k, int(relu), _vp(y),
+                                      C.c_void_p(stream)))
+            acts.append(y)
+            cur = y
+        self._acts = (acts, B, S) if keep else None
+        return cur
+
+    def backward(self, dlogits, stream: int = 0):
+        """Accumulates the parameter gradients of the last kept forward."""
+        torch = _torch()
+        lib = L.lib()
+        acts, B, S = self._acts
+        n = B * S ** 3
+        gviews = self._views(self.grad)
+        pviews = self._views(self.params)
+        dy = dlogits
+        for li in range(len(LAYERS) - 1, -1, -1):
+            cin, cout, k, _ = LAYERS[li]
+            gw, gb = gviews[li]
+            L.check(lib.c2g_cs_conv3d_bwd_weight(_vp(acts[li]), _vp(dy), B, S, S, S, cin, cout, k, _vp(gw),
+                                                 _vp(gb), C.c_void_p(stream)))
+            if li > 0:
+                dx = torch.empty(n * cin, dtype=torch.float32, device="cuda")
+                # acts[li] is the ReLU output of layer li-1: its mask
+                L.check(lib.c2g_cs_conv3d_bwd_data(_vp(dy), B, S, S, S, cout, _vp(pviews[li][0]), cin, k,
+                                                   _vp(acts[li]), _vp(dx), C.c_void_p(stream)))
+                dy = dx
+
+    def adam(self, lr: float, b1=0.9, b2=0.999, eps=1e-8, stream: int = 0):
+        self.t += 1
+        L.check(L.lib().c2g_cs_adam(_vp(self.params), _vp(self.grad), _vp(self.m), _vp(self.v), self.n, lr, b1, b2,
+                                    eps, self.t, C.c_void_p(stream)))
+
+    def rounded(self) -> "SeedNet":
+        """The network with its weights rounded to BF16 values (as stored)."""
+        return SeedNet(params=bf16_round(self.params.cpu().numpy()))
+
+    def save(self, path: str, meta: Optional[dict] = None):
+        p = self.params.cpu().numpy().astype(np.float32)
+        bits = (bf16_round(p).view(np.uint32) >> 16).astype(np.uint16)
+        np.savez_compressed(path, bf16=bits, layers=np.array(LAYERS, np.int32),
+                            meta=json.dumps(meta or {}))
+
+    @classmethod
+    def load(cls, path: str = WEIGHTS) -> "SeedNet":
+        z = np.load(path)
+        if not np.array_equal(z["layers"], np.array(LAYERS, np.int32)):
+            raise ValueError("weights file does not match the network's layers")
+        p = (z["bf16"].astype(np.uint32) << 16).view(np.float32)
+        net = cls(params=p)
+        net.meta = json.loads(str(z["meta"]))
+        return net
+
+
+def loss_and_grad(net: SeedNet, logits, tgt, nvox: int, npos: int, pos_w: float, off_w: float, stream=0):
+    torch = _torch()
+    dl = torch.empty_like(logits)
+    acc = torch.zeros(1, dtype=torch.float64, device="cuda")
+    L.check(L.lib().c2g_cs_loss(_vp(logits), _vp(tgt), nvox, npos, pos_w, off_w, _vp(dl), _vp(acc),
+                                C.c_void_p(stream)))
+    return dl, acc
+
+
+def targets(cps: np.ndarray, B: int, S: int, stream=0):
+    """Dense targets [B*S^3*8] on the GPU from rows (sample, fi, fj, fk, type)."""
+    torch = _torch()
+    tgt = torch.zeros(B * S ** 3 * 8, dtype=torch.float32, device="cuda")
+    if len(cps):
+        d = torch.tensor(np.ascontiguousarray(cps, np.float32).reshape(-1), device="cuda")
+        L.check(L.lib().c2g_cs_targets(_vp(d), len(cps), S, _vp(tgt), C.c_void_p(stream)))
+    return tgt
+
+
+# ------------------------------------------------------------- proposing
+def propose(wfn, net: SeedNet, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: str = "tf32x3",
+            thresh: float = 0.3, local_max: bool = True, cap: int = 1 << 16) -> np.ndarray:
+    """Seeds (n,3) from the network, in voxel order."""
+    torch = _torch()
+    x, x0 = features(wfn, S, h, prec)
+    lg = net.forward(x, 1, S)
+    seeds = torch.empty(cap * 3, dtype=torch.float64, device="cuda")
+    vox = torch.empty(cap, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    tl = float(np.log(thresh / (1.0 - thresh)))
+    L.check(L.lib().c2g_cs_seeds(_vp(lg), S, np.ascontiguousarray(x0, np.float64), h, tl, int(local_max), cap,
+                                 _vp(seeds), _vp(vox), _vp(cnt), None))
+    n = min(int(cnt.item()), cap)
+    s = seeds[: 3 * n].cpu().numpy().reshape(n, 3)
+    v = vox[:n].cpu().numpy()
+    return s[np.argsort(v, kind="stable")]
+
+
+def learned_autocritic(wfn, net: SeedNet, prec: str = "tf32x3", S: int = S_DEFAULT, h: float = H_DEFAULT,
+                       stages=((0.3, True), (0.1, False))) -> dict:
+    """AUTO with learned seeds.  Each stage proposes seeds, runs the
+    confirmed Newton + addcp search and accepts the CP list if its
+    Poincare-Hopf sum is 1; after the last stage the plain pair seeds are
+    the fallback.  Returns the autocritic dict plus `stage` (index of the
+    accepted stage, or 'fallback'), `seeds_used`, `tries` and `ms` (wall
+    time of the whole search)."""
+    torch = _torch()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tries, used = [], 0
+    res = None
+    for i, (th, lm) in enumerate(stages):
+        seeds = propose(wfn, net, S, h, prec, th, lm)
+        used += len(seeds)
+        if len(seeds) == 0:
+            tries.append({"stage": i, "nseed": 0, "ph": None})
+            continue
+        res = wfn.autocritic(seeds, prec)
+        tries.append({"stage": i, "nseed": len(seeds), "ph": int(res["ph"])})
+        if res["ph"] == 1:
+            res["stage"] = i
+            break
+    else:
+        res = wfn.autocritic(None, prec)
+        used += int(res["nseed"])
+        res["stage"] = "fallback"
+    torch.cuda.synchronize()
+    res["ms"] = 1e3 * (time.perf_counter() - t0)
+    res["seeds_used"] = used
+    res["tries"] = tries
+    return res
+
+
+def match_cps(ref: dict, got: dict, tol: float = 1e-3) -> np.ndarray:
+    """For each CP of `ref`, whether `got` has a CP of the same type within
+    tol bohr."""
+    found = np.zeros(len(ref["xyz"]), bool)
+    if len(got["xyz"]) == 0:
+        return found
+    for j, (x, t) in enumerate(zip(ref["xyz"], ref["typ"])):
+        d = np.linalg.norm(got["xyz"] - x, axis=1)
+        i = int(np.argmin(d))
+        found[j] = d[i] <= tol and got["typ"][i] == t
+    return found
+
+
+# -------------------------------------------------------------- training
+@dataclass
+class Sample:
+    x: object           # features on the GPU, [S^3*4]
+    labels: np.ndarray  # (n, 4) fi, fj, fk, type
+    natom: int
+    ncp: int
+    ms_auto: float
+
+
+def make_sample(mol, S: int, h: float, prec: str) -> Sample:
+    from .wfn import Wavefunction
+    w = Wavefunction(mol)
+    try:
+        x, x0 = features(w, S, h, prec)
+        res = w.autocritic(None, prec)
+        lab = cp_labels(res["xyz"], res["typ"], mol.atom_xyz, x0, h, S)
+        return Sample(x, lab, mol.natom, len(res["xyz"]), float(res["ms"]))
+    finally:
+        w.close()
+
+
+def train(samples: List[Sample], epochs: int, batch: int, lr: float, S: int, seed: int = 0,
+          pos_w: float = 10.0, off_w: float = 4.0, log=print) -> SeedNet:
+    torch = _torch()
+    net = SeedNet(seed=seed)
+    rng = np.random.default_rng(seed)
+    nstep = epochs * ((len(samples) + batch - 1) // batch)
+    step = 0
+    for ep in range(epochs):
+        order = rng.permutation(len(samples))
+        tot, nb = 0.0, 0
+        t0 = time.perf_counter()
+        for b0 in range(0, len(order), batch):
+            idx = order[b0:b0 + batch]
+            B = len(idx)
+            x = torch.cat([samples[i].x for i in idx])
+            rows = [np.concatenate([np.full((len(samples[i].labels), 1), bi, np.float32), samples[i].labels], 1)
+                    for bi, i in enumerate(idx)]
+            cps = np.concatenate(rows) if rows else np.zeros((0, 5), np.float32)
+            tgt = targets(cps, B, S)
+            lg = net.forward(x, B, S, keep=True)
+            npos = int(len(cps) * 8)
+            dl, acc = loss_and_grad(net, lg, tgt, B * S ** 3, npos, pos_w, off_w)
+            net.grad.zero_()
+            net.backward(dl)
+            frac = step / max(1, nstep - 1)
+            net.adam(lr * (0.5 * (1.0 + np.cos(np.pi * frac))) + 1e-5)
+            step += 1
+            tot += float(acc.item())
+            nb += 1
+        torch.cuda.synchronize()
+        log(f"epoch {ep}: mean loss {tot / max(nb, 1):.5f}  ({time.perf_counter() - t0:.1f} s)")
+    return net
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train", help="generate training data with plain AUTO and train on the GPU")
+    t.add_argument("--nmol", type=int, default=2000)
+    t.add_argument("--epochs", type=int, default=12)
+    t.add_argument("--batch", type=int, default=4)
+    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--prec", default="tf32x3")
+    t.add_argument("--nval", type=int, default=8)
+    t.add_argument("--out", default=WEIGHTS)
+    t.add_argument("--log", default=None)
+    a = ap.parse_args(argv)
+    logf = open(a.log, "a") if a.log else None
+
+    def log(msg):
+        print(msg, flush=True)
+        if logf:
+            logf.write(msg + "\n")
+            logf.flush()
+
+    if a.cmd == "train":
+        S, h = S_DEFAULT, H_DEFAULT
+        t0 = time.perf_counter()
+        samples = []
+        for i in range(a.nmol):
+            samples.append(make_sample(synth.training_molecule(i), S, h, a.prec))
+            if (i + 1) % max(1, a.nmol // 20) == 0:
+                log(f"data: {i + 1}/{a.nmol} molecules, {time.perf_counter() - t0:.0f} s, "
+                    f"last natom {samples[-1].natom} ncp {samples[-1].ncp} labels {len(samples[-1].labels)}")
+        t_data = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        net = train(samples, a.epochs, a.batch, a.lr, S, log=log)
+        t_train = time.perf_counter() - t1
+        # held-out check against plain AUTO
+        from .wfn import Wavefunction
+        rn = net.rounded()
+        stats = []
+        for j in range(a.nval):
+            mol = synth.training_molecule(10 ** 6 + j)
+            w = Wavefunction(mol)
+            ref = w.autocritic(None, a.prec)
+            got = learned_autocritic(w, rn, a.prec)
+            rec = match_cps(ref, got)
+            stats.append(dict(natom=mol.natom, ncp=len(ref["xyz"]), recall=float(rec.mean()), ph=int(got["ph"]),
+                              stage=got["stage"], seeds=got["seeds_used"], plain_seeds=int(ref["nseed"]),
+                              ms_plain=float(ref["ms"]), ms_learned=float(got["ms"])))
+            log("val " + json.dumps(stats[-1]))
+            w.close()
+        meta = dict(nmol=a.nmol, epochs=a.epochs, batch=a.batch, lr=a.lr, prec=a.prec, S=S, h=h,
+                    s_data=round(t_data, 1), s_train=round(t_train, 1), val=stats)
+        net.save(a.out, meta)
+        log("saved " + a.out + " " + json.dumps({k: v for k, v in meta.items() if k != "val"}))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

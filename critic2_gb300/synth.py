@@ -141,7 +141,24 @@ def _place_atoms(rng, natom: int, box: float, fragments: int, dmin: float = 1.8)
 def make_molecule(name: str, seed: Optional[int] = None) -> Molecule:
     """Builds the named workload's molecule (deterministic for a given seed)."""
     w = WORKLOADS[name]
-    rng = np.random.default_rng(w.seed if seed is None else seed)
+    return build_molecule(w, w.seed if seed is None else seed)
+
+
+def training_molecule(index: int, natom_range=(10, 80)) -> Molecule:
+    """Molecule `index` of the CP-seed proposer's training family: the same
+    construction as cp100 (s/p/d, ~20 primitives and 2 MOs per atom, one
+    fragment, the same atom density) with natom drawn uniformly from
+    natom_range.  Indices >= 10**6 are reserved for held-out molecules."""
+    rng = np.random.default_rng(7_000_000 + index)
+    natom = int(rng.integers(natom_range[0], natom_range[1] + 1))
+    w = Workload(f"train{index}", natom, 20 * natom, None, False, 2 * natom, 0, 0.1, 1,
+                 8_000_000 + index)
+    return build_molecule(w, w.seed)
+
+
+def build_molecule(w: Workload, seed: int) -> Molecule:
+    """The generator behind every workload (see the module doc)."""
+    rng = np.random.default_rng(seed)
     per_heavy = _nprim(_shells(True, w.with_f))
     per_h = _nprim(_shells(False, w.with_f))
     if w.nh is not None:
@@ -177,7 +194,7 @@ def make_molecule(name: str, seed: Optional[int] = None) -> Molecule:
     occ = np.full(w.nmo, 2.0)
     return Molecule(pos, z, np.array(icenter, np.int32), np.array(itype, np.int32),
                     np.array(e, np.float64), occ, np.ascontiguousarray(cmo),
-                    wfntyp=0, nalpha=w.nmo, name=name)
+                    wfntyp=0, nalpha=w.nmo, name=w.name)
 
 
 def nci_grid(mol: Molecule, n: int, step: float):

@@ -37,6 +37,7 @@ class Wavefunction:
 
     def __init__(self, mol=None, *, _handle=None):
         self._h = C.c_void_p()
+        self.atom_xyz = None if mol is None else np.array(mol.atom_xyz, np.float64).reshape(-1, 3)
         if _handle is not None:
             self._h = _handle
         else:

@@ -1,0 +1,244 @@
+"""Learned CP-seed proposer: the hand-written CUDA forward/backward kernels
+against torch's CPU convolution and autograd (the oracle for this part), the
+target/feature/seed/Adam kernels against numpy, and the learned AUTO search
+against the plain one."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from critic2_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def to_torch_w(w, cin, cout, k):
+    """w[tap][cin][cout] -> torch conv3d weight [cout][cin][kz][ky][kx]."""
+    return torch.as_tensor(w).reshape(k, k, k, cin, cout).permute(4, 3, 0, 1, 2).contiguous()
+
+
+def ref_conv(x, w, b, cin, cout, k, relu):
+    """x [B,D,H,W,cin] float64 -> [B,D,H,W,cout] with torch CPU."""
+    y = torch.nn.functional.conv3d(x.permute(0, 4, 1, 2, 3), to_torch_w(w, cin, cout, k),
+                                   None if b is None else torch.as_tensor(b), padding=k // 2)
+    if relu:
+        y = torch.relu(y)
+    return y.permute(0, 2, 3, 4, 1)
+
+
+@pytest.mark.parametrize("cin,cout,k,relu", [(4, 16, 3, True), (16, 32, 3, True), (32, 32, 3, False),
+                                             (32, 8, 1, False)])
+def test_conv_forward_and_backward(gpu_lib, cin, cout, k, relu):
+    L = gpu_lib.lib()
+    rng = np.random.default_rng(cin * 100 + cout)
+    B, D, H, W = 2, 5, 6, 8
+    x = rng.standard_normal((B, D, H, W, cin))
+    w = rng.standard_normal(k ** 3 * cin * cout) * 0.2
+    b = rng.standard_normal(cout) * 0.1
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda").reshape(-1)
+    wd = torch.tensor(w, dtype=torch.float32, device="cuda")
+    bd = torch.tensor(b, dtype=torch.float32, device="cuda")
+    yd = torch.empty(B * D * H * W * cout, dtype=torch.float32, device="cuda")
+    gpu_lib.check(L.c2g_cs_conv3d(_p(xd), B, D, H, W, cin, _p(wd), _p(bd), cout, k, int(relu), _p(yd), None))
+    # oracle in float64 on the CPU
+    xt = torch.tensor(x, dtype=torch.float64, requires_grad=True)
+    wt = torch.tensor(w, dtype=torch.float64, requires_grad=True)
+    bt = torch.tensor(b, dtype=torch.float64, requires_grad=True)
+    yt = ref_conv(xt, wt, bt, cin, cout, k, relu)
+    y = yd.cpu().double().reshape(yt.shape)
+    scale = yt.abs().max().item()
+    assert (y - yt).abs().max().item() <= 2e-5 * scale
+    # backward with an upstream gradient g
+    g = rng.standard_normal(yt.shape)
+    yt.backward(torch.tensor(g))
+    gd = torch.tensor(g, dtype=torch.float32, device="cuda").reshape(-1)
+    if relu:  # the kernels take the ReLU derivative from the stored output
+        gd = gd * (yd > 0).float()
+    dw = torch.zeros_like(wd)
+    db = torch.zeros_like(bd)
+    gpu_lib.check(L.c2g_cs_conv3d_bwd_weight(_p(xd), _p(gd), B, D, H, W, cin, cout, k, _p(dw), _p(db), None))
+    assert (dw.cpu().double() - wt.grad).abs().max().item() <= 2e-5 * wt.grad.abs().max().item()
+    assert (db.cpu().double() - bt.grad).abs().max().item() <= 2e-5 * bt.grad.abs().max().item()
+    if cin % 8 == 0:
+        dx = torch.empty_like(xd)
+        gpu_lib.check(L.c2g_cs_conv3d_bwd_data(_p(gd), B, D, H, W, cout, _p(wd), cin, k, None, _p(dx), None))
+        assert (dx.cpu().double().reshape(xt.shape) - xt.grad).abs().max().item() <= \
+            2e-5 * xt.grad.abs().max().item()
+
+
+def ref_net_loss(x, params, cps, B, S, pos_w, off_w):
+    """The proposer's forward pass and loss in float64 with torch CPU."""
+    from critic2_gb300.cpseed import LAYERS
+    o = 0
+    cur = x
+    ps = []
+    for cin, cout, k, relu in LAYERS:
+        w = params[o:o + k ** 3 * cin * cout]
+        o += k ** 3 * cin * cout
+        b = params[o:o + cout]
+        o += cout
+        ps += [w, b]
+        cur = ref_conv(cur, w, b, cin, cout, k, relu)
+    out = cur.reshape(-1, 8)
+    tgt = np.zeros((B * S ** 3, 8))
+    for r in cps:  # same construction as the targets kernel
+        bi, f, typ = int(r[0]), r[1:4], int(r[4])
+        i0 = np.floor(f).astype(int)
+        for c in range(8):
+            ii = i0 + np.array([(c >> a) & 1 for a in range(3)])
+            if np.all(ii >= 0) and np.all(ii < S):
+                v = ((bi * S + ii[0]) * S + ii[1]) * S + ii[2]
+                tgt[v, typ] = 1
+                tgt[v, 4:7] = f - ii
+                tgt[v, 7] = 1
+    tgt = torch.tensor(tgt)
+    z, y = out[:, :4], tgt[:, :4]
+    wgt = torch.where(y > 0.5, pos_w, 1.0)
+    nvox = out.shape[0]
+    npos = len(cps) * 8
+    loss = (wgt * (torch.nn.functional.softplus(z) - z * y)).sum() / nvox
+    m = tgt[:, 7:8]
+    loss = loss + 0.5 * off_w * (m * (out[:, 4:7] - tgt[:, 4:7]) ** 2).sum() / max(1, npos)
+    return loss, tgt
+
+
+def test_network_gradient_check(gpu_lib):
+    """Forward, loss and backward of the whole network on the GPU against
+    torch CPU autograd (float64): every parameter's gradient."""
+    from critic2_gb300 import cpseed
+    rng = np.random.default_rng(5)
+    B, S = 2, 8
+    net = cpseed.SeedNet(seed=3)
+    x = rng.standard_normal((B, S, S, S, 4)) * 0.7
+    cps = np.array([[0, 2.3, 4.1, 5.7, 1], [1, 1.5, 6.2, 3.3, 2], [1, 6.9, 0.4, 2.2, 3], [0, 5.5, 5.5, 1.0, 0]],
+                   np.float32)
+    pos_w, off_w = 10.0, 4.0
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda").reshape(-1)
+    lg = net.forward(xd, B, S, keep=True)
+    tgt = cpseed.targets(cps, B, S)
+    dl, acc = cpseed.loss_and_grad(net, lg, tgt, B * S ** 3, len(cps) * 8, pos_w, off_w)
+    net.grad.zero_()
+    net.backward(dl)
+    torch.cuda.synchronize()
+    p = torch.tensor(net.params.cpu().numpy().astype(np.float64), requires_grad=True)
+    loss, tref = ref_net_loss(torch.tensor(x), p, cps, B, S, pos_w, off_w)
+    loss.backward()
+    assert np.allclose(tgt.cpu().numpy().reshape(-1, 8), tref.numpy(), atol=1e-6)
+    assert abs(acc.item() - loss.item()) <= 1e-5 * abs(loss.item())
+    g = net.grad.cpu().double()
+    o = 0
+    for cin, cout, k, _ in cpseed.LAYERS:
+        for n in (k ** 3 * cin * cout, cout):
+            a, r = g[o:o + n], p.grad[o:o + n]
+            assert (a - r).abs().max().item() <= 1e-4 * max(r.abs().max().item(), 1e-12), (cin, cout, n)
+            o += n
+
+
+def test_adam_step(gpu_lib):
+    L = gpu_lib.lib()
+    rng = np.random.default_rng(2)
+    n = 1000
+    p, g = rng.standard_normal(n), rng.standard_normal(n)
+    m, v = rng.standard_normal(n) * 0.1, rng.random(n) * 0.1
+    pd, gd, md, vd = (torch.tensor(a, dtype=torch.float32, device="cuda") for a in (p, g, m, v))
+    gpu_lib.check(L.c2g_cs_adam(_p(pd), _p(gd), _p(md), _p(vd), n, 1e-3, 0.9, 0.999, 1e-8, 3, None))
+    m2 = 0.9 * m + 0.1 * g
+    v2 = 0.999 * v + 0.001 * g * g
+    p2 = p - 1e-3 * (m2 / (1 - 0.9 ** 3)) / (np.sqrt(v2 / (1 - 0.999 ** 3)) + 1e-8)
+    assert np.allclose(pd.cpu().numpy(), p2, rtol=1e-5, atol=1e-6)
+
+
+def test_features_and_seeds(gpu_lib):
+    from critic2_gb300 import cpseed
+    L = gpu_lib.lib()
+    rng = np.random.default_rng(9)
+    S = 8
+    n = S ** 3
+    crho = rng.standard_normal(n) * 10.0 ** rng.uniform(-10, 3, n)
+    cgrad = 10.0 ** rng.uniform(-6, 3, n)
+    cd, gd = torch.tensor(crho, device="cuda"), torch.tensor(cgrad, device="cuda")
+    xd = torch.empty(n * 4, dtype=torch.float32, device="cuda")
+    gpu_lib.check(L.c2g_cs_features(_p(cd), _p(gd), n, _p(xd), None))
+    x = xd.cpu().numpy().reshape(n, 4)
+    lr = np.log10(np.maximum(np.abs(crho) / 100, 1e-30))
+    assert np.allclose(x[:, 0], (np.clip(lr, -12, 4) + 4) / 4, atol=1e-5)
+    assert np.array_equal(x[:, 1], np.sign(crho).astype(np.float32))
+    assert np.allclose(x[:, 2], -np.clip(np.log10(np.maximum(cgrad, 1e-4)), -4, 2) / 2, atol=1e-5)
+    # seeds: threshold and 26-neighbour maxima on random logits
+    lg = rng.standard_normal((n, 8)).astype(np.float32)
+    lgd = torch.tensor(lg.reshape(-1), device="cuda")
+    x0 = np.array([1.0, -2.0, 0.5])
+    h = 0.45
+    for thr, lm in ((1.0, 1), (1.5, 0)):
+        seeds = torch.empty(3 * n, dtype=torch.float64, device="cuda")
+        vox = torch.empty(n, dtype=torch.int32, device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        gpu_lib.check(L.c2g_cs_seeds(_p(lgd), S, x0, h, thr, lm, n, _p(seeds), _p(vox), _p(cnt), None))
+        k = int(cnt.item())
+        got = {int(v): seeds[3 * i:3 * i + 3].cpu().numpy() for i, v in enumerate(vox[:k].cpu().numpy())}
+        p = lg[:, :4].max(1).reshape(S, S, S)
+        want = {}
+        for v in range(n):
+            i, j, kk = v // (S * S), (v // S) % S, v % S
+            if not p[i, j, kk] > thr:
+                continue
+            if lm:
+                ok = True
+                for di in (-1, 0, 1):
+                    for dj in (-1, 0, 1):
+                        for dk in (-1, 0, 1):
+                            a, b, c = i + di, j + dj, kk + dk
+                            if (di, dj, dk) == (0, 0, 0) or min(a, b, c) < 0 or max(a, b, c) >= S:
+                                continue
+                            u = (a * S + b) * S + c
+                            if p[a, b, c] > p[i, j, kk] or (p[a, b, c] == p[i, j, kk] and u < v):
+                                ok = False
+                if not ok:
+                    continue
+            off = np.clip(lg[v, 4:7], -1.5, 1.5)
+            want[v] = x0 + h * (np.array([i, j, kk]) + off)
+        assert set(got) == set(want)
+        for v in want:
+            assert np.allclose(got[v], want[v], atol=1e-6)
+
+
+@pytest.fixture(scope="module")
+def trained():
+    from critic2_gb300 import cpseed
+    if not os.path.exists(cpseed.WEIGHTS):
+        pytest.skip("no trained weights in the package")
+    return cpseed.SeedNet.load()
+
+
+def test_learned_autocritic_vs_plain(gpu_lib, trained):
+    """On held-out molecules of the training family the learned search finds
+    every CP of the plain search, passes Poincare-Hopf, and needs far fewer
+    Newton seeds; an untrained network finds nothing useful and the search
+    falls back to the plain seeds (same CPs)."""
+    from critic2_gb300 import cpseed
+    from critic2_gb300.wfn import Wavefunction
+    untrained = cpseed.SeedNet(seed=11).rounded()
+    for j in range(2):
+        mol = synth.training_molecule(10 ** 6 + 100 + j, natom_range=(20, 40))
+        w = Wavefunction(mol)
+        ref = w.autocritic(None, "tf32x3")
+        got = cpseed.learned_autocritic(w, trained, "tf32x3")
+        rec = cpseed.match_cps(ref, got)
+        print(f"\nnatom {mol.natom}: plain {len(ref['xyz'])} CPs from {ref['nseed']} seeds in {ref['ms']:.0f} ms; "
+              f"learned recall {rec.mean():.3f}, PH {got['ph']}, stage {got['stage']}, "
+              f"{got['seeds_used']} seeds, {got['ms']:.0f} ms")
+        assert got["ph"] == 1 or got["stage"] == "fallback"
+        if got["stage"] != "fallback":
+            assert got["seeds_used"] < ref["nseed"]
+        base = cpseed.learned_autocritic(w, untrained, "tf32x3", stages=((0.9, True),))
+        assert base["stage"] == "fallback" or base["ph"] == 1
+        if base["stage"] == "fallback":
+            assert cpseed.match_cps(ref, base).all()
+        w.close()
