@@ -4,14 +4,19 @@
 //   phi_c(mo, p) = sum_k cmo(mo, k) * chi_c(k, p),  c = value, 3 first and
 //   6 second derivatives,
 // followed by the MO reduction of rho2 (src/wfn_private@proc.F90:2546-2624).
-// Here it runs as 10 tcgen05 MMAs per K-step with
+// Here it runs on tcgen05 MMAs with
 //   M = 128 MOs (A = the coefficient tile, resident in tensor memory),
-//   N = 32 points (B = the basis block chi, built in shared memory),
+//   N = (component, point) pairs of half a 32-point tile (B = the basis block
+//       chi built in shared memory, one row per component and point, so one
+//       N = 160 MMA takes all ten components of 16 points),
 //   K = one 32-byte row of primitives (16 bf16 or 8 tf32),
-// in a 3-product split: A_hi*B_hi + A_hi*B_lo + A_lo*B_hi, FP32 accumulate.
-// The accumulators (10 x 32 columns for the hi*hi products, 4 x 32 for the
-// cross products of the value and gradient) and 4 coefficient stages (16
-// columns each) fill the SM's 512 TMEM columns.
+// in a 3-product split: A_hi*B_hi + A_hi*B_lo + A_lo*B_hi, FP32 accumulate;
+// per K-step and half-tile five MMAs: hi*hi (N = 160), the two cross
+// products of the value and gradient (N = 64, own accumulator) and of the
+// second derivatives (N = 96, into the main accumulator).  The accumulators
+// (2 x 160 columns for the hi*hi products, 2 x 64 for the cross products
+// of the value and gradient) and 4 coefficient stages (16 columns each)
+// fill the SM's 512 TMEM columns.
 //
 // CTA roles (persistent, one CTA per SM, 12 warps):
 //   warps 0-3  load the coefficient stage (L2 -> registers -> tcgen05.st into
@@ -86,26 +91,37 @@ struct TcOperands {
 
 namespace {
 namespace K {
-constexpr int NP = 32;     // points per tile (MMA N)
+constexpr int NP = 32;     // points per tile
 constexpr int MT = 128;    // MOs per tile (MMA M)
 constexpr int NCOMP = 10;  // value, 3 first, 6 second derivatives
-constexpr int PIECE = NP * 32;            // bytes of one (component, piece) B tile
-constexpr int STAGE = NCOMP * 2 * PIECE;  // bytes of one K-stage
+// The tile's points form two halves of 16; for each half the B operand has
+// one row per (component, point): row = component * 16 + point, so that a
+// single N = 160 MMA covers all ten components of a half (small-N MMAs
+// run at a fraction of the tensor pipe's rate).
+constexpr int NH = 2;                   // point halves per tile
+constexpr int HP = NP / NH;             // 16 points per half
+constexpr int BROWS = NCOMP * HP;       // 160 B rows per half
+constexpr int BPIECE = BROWS * 32;      // 5120 bytes: one (half, hi|lo) B operand
+constexpr int STAGE = NH * 2 * BPIECE;  // bytes of one K-stage (20480)
 constexpr int NSTAGE = 6;  // shared-memory basis-block stages
 constexpr int NCBUF = 4;   // coefficient buffers in TMEM
 constexpr int NPROD = 6;
 constexpr int W_MMA = 4, W_SETUP = 5, W_PROD0 = 6;
 constexpr int NTHR = (W_PROD0 + NPROD) * 32;  // 384
 constexpr uint32_t TMEM_COLS = 512;
-// TMEM columns: accumulators of the hi*hi products for the 10 components,
-// accumulators of the cross products (hi*lo + lo*hi) for the value and the
-// gradient, then the coefficient buffers.  Keeping the small cross terms
-// apart means the large accumulator takes one truncating addition per MMA
-// step instead of three (the tensor core's FP32 accumulation rounds toward
-// zero, so the error grows with the number of additions).
+// TMEM columns: per half, the accumulators of the hi*hi products of the 10
+// components (160 columns, column = component * 16 + point), then per half
+// the accumulators of the cross products (hi*lo + lo*hi) of the value and
+// the gradient (64 columns), then the coefficient buffers.  Keeping the
+// small cross terms apart means the large accumulator takes one truncating
+// addition per MMA step instead of three (the tensor core's FP32
+// accumulation rounds toward zero, so the error grows with the number of
+// additions); the cross terms of the second derivatives go into the main
+// accumulator.
 constexpr int NXCOMP = 4;
-constexpr int XCOL0 = NCOMP * NP;           // 320
-constexpr int CBUF0 = XCOL0 + NXCOMP * NP;  // 448
+constexpr int XROWS = NXCOMP * HP;          // 64
+constexpr int XCOL0 = NH * BROWS;           // 320
+constexpr int CBUF0 = XCOL0 + NH * XROWS;   // 448
 static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
 constexpr uint64_t TIMEOUT_NS = 4000000000ull;
@@ -407,12 +423,15 @@ __device__ __noinline__ void produce_half(const StageRow *rows, int half, const 
       }
     }
   }
-  uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
+  // point r = half-tile hf, row p; B row of component c = c * 16 + p, whose
+  // 8-row group is 2c + (p >> 3)
+  const int hf = r >> 4, p = r & 15;
+  uint8_t *row = dst + hf * (2 * K::BPIECE) + (p >> 3) * 256 + half * 128 + (p & 7) * 16;
 #pragma unroll
   for (int c = 0; c < 10; c++)
 #pragma unroll
     for (int pc = 0; pc < 2; pc++)
-      *reinterpret_cast<uint4 *>(row + (c * 2 + pc) * K::PIECE) =
+      *reinterpret_cast<uint4 *>(row + pc * K::BPIECE + c * 512) =
           make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
 }
 
@@ -715,7 +734,10 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
   } else if (warp == K::W_MMA) {
     // ------------------------------------------------------------ MMA issue
     if (lane == 0) {
-      constexpr uint32_t idesc = ptx::make_idesc(KIND == 0 ? 1 : 2, K::MT, K::NP);
+      constexpr uint32_t fmt = KIND == 0 ? 1 : 2;
+      constexpr uint32_t id_all = ptx::make_idesc(fmt, K::MT, K::BROWS);           // 10 components
+      constexpr uint32_t id_x = ptx::make_idesc(fmt, K::MT, K::XROWS);             // components 0-3
+      constexpr uint32_t id_h = ptx::make_idesc(fmt, K::MT, K::BROWS - K::XROWS);  // components 4-9
       uint32_t g = 0, u = 0;
       bool ok = true;
       for (int t = 0; t < ntl && ok; t++) {
@@ -736,20 +758,27 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
             const uint32_t sb = ptx::smem_u32(s.stage + b * K::STAGE);
             const uint32_t acc0 = j > 0 ? 1u : 0u;
 #pragma unroll
-            for (int c = 0; c < K::NCOMP; c++) {
-              const uint32_t dcol = tmem + c * K::NP;
-              const uint32_t xcol = c < K::NXCOMP ? tmem + K::XCOL0 + c * K::NP : dcol;
-              const uint32_t xacc = c < K::NXCOMP ? acc0 : 1u;
-              const uint64_t bh = ptx::smem_desc_kmajor(sb + (2 * c) * K::PIECE, 128, 256);
-              const uint64_t bl = ptx::smem_desc_kmajor(sb + (2 * c + 1) * K::PIECE, 128, 256);
+            for (int hf = 0; hf < K::NH; hf++) {
+              const uint32_t dcol = tmem + hf * K::BROWS, xcol = tmem + K::XCOL0 + hf * K::XROWS;
+              const uint32_t sh = sb + hf * 2 * K::BPIECE, sl = sh + K::BPIECE;
+              const uint64_t bh = ptx::smem_desc_kmajor(sh, 128, 256);
+              const uint64_t bl = ptx::smem_desc_kmajor(sl, 128, 256);
+              // rows 64-159 (components 4-9) start 8 row groups in
+              const uint64_t bh2 = ptx::smem_desc_kmajor(sh + 8 * 256, 128, 256);
+              const uint64_t bl2 = ptx::smem_desc_kmajor(sl + 8 * 256, 128, 256);
+              const uint32_t dcol2 = dcol + K::XROWS;
               if constexpr (KIND == 0) {
-                ptx::mma_bf16_ts(dcol, a_hi, bh, idesc, acc0);
-                ptx::mma_bf16_ts(xcol, a_hi, bl, idesc, xacc);
-                ptx::mma_bf16_ts(xcol, a_lo, bh, idesc, 1u);
+                ptx::mma_bf16_ts(dcol, a_hi, bh, id_all, acc0);
+                ptx::mma_bf16_ts(xcol, a_hi, bl, id_x, acc0);
+                ptx::mma_bf16_ts(xcol, a_lo, bh, id_x, 1u);
+                ptx::mma_bf16_ts(dcol2, a_hi, bl2, id_h, 1u);
+                ptx::mma_bf16_ts(dcol2, a_lo, bh2, id_h, 1u);
               } else {
-                ptx::mma_tf32_ts(dcol, a_hi, bh, idesc, acc0);
-                ptx::mma_tf32_ts(xcol, a_hi, bl, idesc, xacc);
-                ptx::mma_tf32_ts(xcol, a_lo, bh, idesc, 1u);
+                ptx::mma_tf32_ts(dcol, a_hi, bh, id_all, acc0);
+                ptx::mma_tf32_ts(xcol, a_hi, bl, id_x, acc0);
+                ptx::mma_tf32_ts(xcol, a_lo, bh, id_x, 1u);
+                ptx::mma_tf32_ts(dcol2, a_hi, bl2, id_h, 1u);
+                ptx::mma_tf32_ts(dcol2, a_lo, bh2, id_h, 1u);
               }
             }
             ptx::mma_commit(&s.bar[K::B_EMPTY + b]);
@@ -844,10 +873,13 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
 #pragma unroll 1
           for (int ch = 0; ch < 4; ch++) {
             uint32_t v[10][8], xv[K::NXCOMP][8];
+            // points ch*8 .. ch*8+7: half ch/2, rows (ch%2)*8 ..
+            const uint32_t dc = tmem + lanebase + (ch >> 1) * K::BROWS + (ch & 1) * 8;
+            const uint32_t xc = tmem + lanebase + K::XCOL0 + (ch >> 1) * K::XROWS + (ch & 1) * 8;
 #pragma unroll
-            for (int c = 0; c < 10; c++) ptx::tmem_ld8(tmem + lanebase + c * K::NP + ch * 8, v[c]);
+            for (int c = 0; c < 10; c++) ptx::tmem_ld8(dc + c * K::HP, v[c]);
 #pragma unroll
-            for (int c = 0; c < K::NXCOMP; c++) ptx::tmem_ld8(tmem + lanebase + K::XCOL0 + c * K::NP + ch * 8, xv[c]);
+            for (int c = 0; c < K::NXCOMP; c++) ptx::tmem_ld8(xc + c * K::HP, xv[c]);
             ptx::tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 8; j++) {
