@@ -173,6 +173,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--grid", type=int, default=0, help="grid points per axis (default: the workload's)")
+    ap.add_argument("--binned", action="store_true", help="FP64 comparison binned by rho decade")
     args = ap.parse_args()
     wl = synth.WORKLOADS[args.workload]
     if args.grid > 0:
@@ -275,6 +276,21 @@ def main():
         fp64 = {"value": npts / (t64 / 1e3), "unit": "points/s", "ms_per_step": t64,
                 "speedup_split_vs_fp64": t64 / ms, "max_rel_drho": drel, "max_abs_ds": ds,
                 "sign_flips": flips}
+        if args.binned:
+            # errors against FP64 binned by rho decade
+            lg = torch.floor(torch.log10(rho64.clamp_min(1e-300)))
+            bins = {}
+            for d in range(-8, 4):
+                m = lg == d
+                n = int(m.sum().item())
+                if n == 0:
+                    continue
+                bins[f"1e{d}"] = {
+                    "points": n,
+                    "max_rel_drho": ((rho - rho64).abs() / rho64)[m].max().item(),
+                    "max_abs_ds": (cgrad - gf).abs()[m].max().item(),
+                    "sign_flips": int((torch.sign(crho) != torch.sign(rf))[m].sum().item())}
+            fp64["by_rho_decade"] = bins
     pk, pk_kind = peaks()
     flops = 20.0 * mol.nmo * w.npri * npts  # algorithmic, dense, per step
     achieved = flops / (ms_kernel / 1e3) / 1e12
