@@ -9,7 +9,11 @@ with CUDA events with the outputs in device memory; `e2e` times the public
 C-ABI call that writes host arrays (device->host copy of both cubes inside
 the timed region).  The split-precision path is the measured one; its
 error against the FP64 plain form and the FP64 form's own throughput are
-reported beside it.
+reported beside it.  `cp_search` holds the metric's second part: the wall
+time of AUTO's critical-point search on the 100-atom molecule with critic2's
+pair seeds and with the learned seeds (recall of the plain CP list,
+Poincare-Hopf sums, seeds used), in FP64 and in TF32x3 with FP64 final
+Newton steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--prec MODE]
                   [--workload NAME] [--impl ours|reference]
@@ -162,6 +166,26 @@ def run_reference(args, wl, mol):
     return 0
 
 
+def cp_search(args):
+    """Second half of the metric: AUTO's CP search on the 100-atom molecule
+    (cp100: 1996 primitives, 200 MOs), critic2's pair seeds against the
+    learned seeds, wall time of the whole search through the public API."""
+    from critic2_gb300 import cpseed
+    if not os.path.exists(cpseed.WEIGHTS):
+        return None
+    mol = synth.make_molecule("cp100")
+    net = cpseed.SeedNet.load()
+    out = {"workload": f"cp100: {mol.natom} atoms, {mol.npri} primitives, {mol.nmo} MOs; "
+                       f"proposer on a {cpseed.S_DEFAULT}^3 grid at {cpseed.H_DEFAULT} bohr",
+           "unit": "ms", "higher_is_better": False}
+    for prec in args.cp_prec.split(","):
+        st = cpseed.evaluate(mol, net, prec)
+        out[prec] = {k: st[k] for k in ("ms_plain", "ms_learned", "speedup", "recall", "recall_outside_cores",
+                                        "ncp", "ncp_outside_cores", "plain_ph", "learned_ph", "stage", "reason",
+                                        "plain_seeds", "learned_seeds", "proposal", "grid_seeds")}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -174,6 +198,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--grid", type=int, default=0, help="grid points per axis (default: the workload's)")
     ap.add_argument("--binned", action="store_true", help="FP64 comparison binned by rho decade")
+    ap.add_argument("--no-cp", action="store_true", help="skip the CP-search part")
+    ap.add_argument("--fp64-planes", type=int, default=0, help="FP64 comparison on this many i-planes")
+    ap.add_argument("--cp-prec", default="fp64,tf32x3")
     args = ap.parse_args()
     wl = synth.WORKLOADS[args.workload]
     if args.grid > 0:
@@ -260,14 +287,22 @@ def main():
     # FP64 plain form beside it, and the split-precision error against it
     fp64 = None
     if prec != "fp64" and not args.no_fp64:
+        # FP64 on the whole grid, or on --fp64-planes i-planes from the middle
+        n1, plane = int(ns[0]), int(ns[1]) * int(ns[2])
+        npl = n1 if args.fp64_planes <= 0 else min(n1, args.fp64_planes)
+        i0 = (n1 - npl) // 2
+        x0p = x0 + i0 * xm[:, 0]
+        nsp = np.array([npl, ns[1], ns[2]], np.int32)
+        crho = crho[i0 * plane:(i0 + npl) * plane]
+        cgrad = cgrad[i0 * plane:(i0 + npl) * plane]
         rf = torch.empty_like(crho)
         gf = torch.empty_like(cgrad)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        w.nciplot_dev(x0, xm, ns, "fp64", rf.data_ptr(), gf.data_ptr(), sp)
+        w.nciplot_dev(x0p, xm, nsp, "fp64", rf.data_ptr(), gf.data_ptr(), sp)
         b.record(stream)
         torch.cuda.synchronize()
-        t64 = a.elapsed_time(b)
+        t64 = a.elapsed_time(b) * n1 / npl  # per full grid
         rho64 = rf.abs() / 100
         rho = crho.abs() / 100
         drel = ((rho - rho64).abs() / rho64.clamp_min(1e-300)).max().item()
@@ -275,7 +310,8 @@ def main():
         flips = int((torch.sign(crho) != torch.sign(rf)).sum().item())
         fp64 = {"value": npts / (t64 / 1e3), "unit": "points/s", "ms_per_step": t64,
                 "speedup_split_vs_fp64": t64 / ms, "max_rel_drho": drel, "max_abs_ds": ds,
-                "sign_flips": flips}
+                "sign_flips": flips, "compared_points": int(npl * plane),
+                "sample": "whole grid" if npl == n1 else f"{npl} of {n1} i-planes (time scaled to the grid)"}
         if args.binned:
             # errors against FP64 binned by rho decade
             lg = torch.floor(torch.log10(rho64.clamp_min(1e-300)))
@@ -319,6 +355,10 @@ def main():
             "fp64_recheck_points": nrecheck}
     if fp64:
         line["fp64_plain"] = fp64
+    if rank == 0 and not args.no_cp:
+        cps = cp_search(args)
+        if cps:
+            line["cp_search"] = cps
     if rank == 0 and world == 1 and not args.no_cpu:
         v, cores, sample = cpu_sample(mol, wl)
         line["cpu_baseline"] = {"value": v, "unit": "points/s", "cores": cores, "kind": "port",

@@ -7,17 +7,18 @@ small 3D convolutional network reads a coarse grid of the density and
 proposes a few seeds per critical point; the seeds go through the unchanged
 Newton + addcp stages (`Wavefunction.autocritic(seeds)`), so every CP it
 reports is confirmed by exact-field (FP64-finished) Newton convergence and
-addcp's gradient check.  The result is accepted only if the CP list
-satisfies the Poincare-Hopf sum n - b + r - c = 1; otherwise the search is
-repeated with a denser seed set and, if that fails too, with critic2's
-plain pair seeds (the fallback).
+addcp's gradient check.  The result is accepted if the CP list satisfies
+the Poincare-Hopf sum n - b + r - c = 1; otherwise the search is repeated
+with a denser seed set and accepted if that satisfies the sum or finds no
+new CP outside the nuclear cores; if both fail, critic2's plain pair seeds
+are the fallback.
 
 Pieces (all GPU work goes through the library's kernels; torch only holds
 device memory and streams):
   coarse_grid / features  the S^3 grid (spacing h, centred on the molecule)
                           evaluated by the NCI kernel (c2g_nciplot_dev),
                           turned into 4 input channels (c2g_cs_features);
-  SeedNet                 5 convolutions 4-16-32-32-32 (3^3, ReLU) and a
+  SeedNet                 5 convolutions 4-16-32-32-32-32 (3^3, ReLU) and a
                           1^3 head to 8 channels (4 CP-type heat-map logits,
                           3 sub-voxel offsets); forward, backward and Adam
                           are the library's c2g_cs_* kernels; weights are
@@ -48,7 +49,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "cpseed_weights.npz")
 
 # (cin, cout, ksize, relu)
-LAYERS = ((4, 16, 3, True), (16, 32, 3, True), (32, 32, 3, True), (32, 32, 3, True), (32, 8, 1, False))
+LAYERS = ((4, 16, 3, True), (16, 32, 3, True), (32, 32, 3, True), (32, 32, 3, True), (32, 32, 3, True),
+          (32, 8, 1, False))
 TYPE_OF_SIGNATURE = {-3: 0, -1: 1, 1: 2, 3: 3}  # non-nuclear maximum, bond, ring, cage
 S_DEFAULT, H_DEFAULT = 64, 0.45
 
@@ -100,17 +102,17 @@ def _atoms(wfn) -> np.ndarray:
 
 
 def cp_labels(xyz: np.ndarray, typ: np.ndarray, atom_xyz: np.ndarray, x0: np.ndarray, h: float,
-              S: int, nuc_tol: float = 0.05) -> np.ndarray:
-    """Training targets from a CP list: rows (fi, fj, fk, type) for every
-    non-nuclear CP inside the grid, in fractional voxel coordinates; nuclei
-    (CPs of signature -3 within nuc_tol of an atom) are not learned, AUTO
-    adds them itself."""
+              S: int, core: float = 0.5) -> np.ndarray:
+    """Training targets from a CP list: rows (fi, fj, fk, type) for every CP
+    inside the grid and outside the nuclear cores (within `core` bohr of a
+    nucleus: the nuclei themselves, which AUTO adds on its own, and the
+    rounding-dependent core CPs), in fractional voxel coordinates."""
     rows = []
     for x, t in zip(np.asarray(xyz).reshape(-1, 3), np.asarray(typ)):
         t = int(t)
         if t not in TYPE_OF_SIGNATURE:
             continue
-        if t == -3 and np.min(np.linalg.norm(atom_xyz - x, axis=1)) < nuc_tol:
+        if np.min(np.linalg.norm(atom_xyz - x, axis=1)) < core:
             continue
         f = (x - x0) / h
         if np.all(f >= 0) and np.all(f <= S - 1):
@@ -242,17 +244,37 @@ def targets(cps: np.ndarray, B: int, S: int, stream=0):
 
 
 # ------------------------------------------------------------- proposing
-def propose(wfn, net: SeedNet, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: str = "tf32x3",
-            thresh: float = 0.3, local_max: bool = True, cap: int = 1 << 16) -> np.ndarray:
-    """Seeds (n,3) from the network, in voxel order."""
-    torch = _torch()
+CORE_RADIUS = 0.5  # bohr
+
+
+def core_mask(xyz: np.ndarray, atom_xyz: np.ndarray, r: float = CORE_RADIUS) -> np.ndarray:
+    """CPs within r of a nucleus.  In these cores the density reaches 10^2-10^3
+    and the FP64 rounding of |grad rho| is of the order of AUTO's 1e-12
+    convergence threshold, so whether Newton converges there depends on
+    rounding (two FP64 codes with different summation orders find different
+    core CPs)."""
+    xyz = np.asarray(xyz).reshape(-1, 3)
+    if len(xyz) == 0:
+        return np.zeros(0, bool)
+    d = np.linalg.norm(xyz[:, None, :] - atom_xyz[None, :, :], axis=2).min(1)
+    return d < r
+
+
+def proposer_logits(wfn, net: SeedNet, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: str = "tf32x3"):
     x, x0 = features(wfn, S, h, prec)
-    lg = net.forward(x, 1, S)
+    return net.forward(x, 1, S), x0
+
+
+def seeds_from_logits(lg, x0, S: int = S_DEFAULT, h: float = H_DEFAULT, thresh: float = 0.3,
+                      mode: int = 2, cap: int = 1 << 17) -> np.ndarray:
+    """Seeds (n,3) from the network output, in voxel order (mode: see
+    c2g_cs_seeds; 2 = per-type maxima of the heat maps)."""
+    torch = _torch()
     seeds = torch.empty(cap * 3, dtype=torch.float64, device="cuda")
     vox = torch.empty(cap, dtype=torch.int32, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
     tl = float(np.log(thresh / (1.0 - thresh)))
-    L.check(L.lib().c2g_cs_seeds(_vp(lg), S, np.ascontiguousarray(x0, np.float64), h, tl, int(local_max), cap,
+    L.check(L.lib().c2g_cs_seeds(_vp(lg), S, np.ascontiguousarray(x0, np.float64), h, tl, int(mode), cap,
                                  _vp(seeds), _vp(vox), _vp(cnt), None))
     n = min(int(cnt.item()), cap)
     s = seeds[: 3 * n].cpu().numpy().reshape(n, 3)
@@ -260,38 +282,103 @@ def propose(wfn, net: SeedNet, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: s
     return s[np.argsort(v, kind="stable")]
 
 
-def learned_autocritic(wfn, net: SeedNet, prec: str = "tf32x3", S: int = S_DEFAULT, h: float = H_DEFAULT,
-                       stages=((0.3, True), (0.1, False))) -> dict:
-    """AUTO with learned seeds.  Each stage proposes seeds, runs the
-    confirmed Newton + addcp search and accepts the CP list if its
-    Poincare-Hopf sum is 1; after the last stage the plain pair seeds are
-    the fallback.  Returns the autocritic dict plus `stage` (index of the
-    accepted stage, or 'fallback'), `seeds_used`, `tries` and `ms` (wall
-    time of the whole search)."""
+def cluster_seeds(seeds: np.ndarray, cell: float = 0.2) -> np.ndarray:
+    """Keeps the first seed (in the given order) of every cubic cell of edge
+    `cell` bohr: voxels around one CP predict nearly the same position, so
+    this leaves about one seed per predicted CP."""
+    if len(seeds) == 0:
+        return seeds
+    key = np.floor(seeds / cell).astype(np.int64)
+    _, first = np.unique(key, axis=0, return_index=True)
+    return seeds[np.sort(first)]
+
+
+def grid_seeds(wfn, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: str = "tf32x3") -> np.ndarray:
+    """Non-learned seeds: coarse-grid voxels where the reduced density
+    gradient s (zero at every CP) is a minimum over the 26 neighbours."""
+    torch = _torch()
+    x0, xm, ns = coarse_grid(_atoms(wfn), S, h)
+    crho = torch.empty(S ** 3, dtype=torch.float64, device="cuda")
+    cgrad = torch.empty(S ** 3, dtype=torch.float64, device="cuda")
+    wfn.nciplot_dev(x0, xm, ns, prec, crho.data_ptr(), cgrad.data_ptr(), 0)
+    g = cgrad.cpu().numpy().reshape(S, S, S)
+    pad = np.pad(g, 1, constant_values=np.inf)
+    m = np.ones_like(g, bool)
+    for di in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            for dk in (-1, 0, 1):
+                if (di, dj, dk) != (0, 0, 0):
+                    m &= g <= pad[1 + di:1 + di + S, 1 + dj:1 + dj + S, 1 + dk:1 + dk + S]
+    idx = np.argwhere(m)
+    return x0 + h * idx.astype(np.float64)
+
+
+def propose(wfn, net: SeedNet, S: int = S_DEFAULT, h: float = H_DEFAULT, prec: str = "tf32x3",
+            thresh: float = 0.3, mode: int = 2) -> np.ndarray:
+    lg, x0 = proposer_logits(wfn, net, S, h, prec)
+    return seeds_from_logits(lg, x0, S, h, thresh, mode)
+
+
+def learned_autocritic(wfn, net: SeedNet, prec: str = "fp64", S: int = S_DEFAULT, h: float = H_DEFAULT,
+                       thresh=(0.3, 0.05), cell: float = 0.2, feat_prec: str = "tf32x3") -> dict:
+    """AUTO with learned seeds, confirmed and checked.
+
+    Seeds: every voxel whose heat map exceeds thresh[0], moved by its
+    predicted offset, clustered to one seed per `cell`-bohr cell.  Newton +
+    addcp confirm every CP with the exact field.
+    Check: accepted if the Poincare-Hopf sum n - b + r - c is 1; otherwise
+    the seeds added by lowering the threshold to thresh[1] (those not in an
+    already used cell) run a second search, and the CP list is accepted if
+    that finds no CP outside the nuclear cores that the first one missed
+    (stable under densification); else critic2's plain pair seeds are the
+    fallback.  Returns the autocritic dict of the accepted list plus `stage`
+    ('learned', 'learned+dense' or 'fallback'), `reason`, `seeds_used`,
+    `tries` and `ms` (wall time of the whole search, features and network
+    included)."""
     torch = _torch()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    tries, used = [], 0
-    res = None
-    for i, (th, lm) in enumerate(stages):
-        seeds = propose(wfn, net, S, h, prec, th, lm)
-        used += len(seeds)
-        if len(seeds) == 0:
-            tries.append({"stage": i, "nseed": 0, "ph": None})
-            continue
-        res = wfn.autocritic(seeds, prec)
-        tries.append({"stage": i, "nseed": len(seeds), "ph": int(res["ph"])})
-        if res["ph"] == 1:
-            res["stage"] = i
-            break
-    else:
+    lg, x0 = proposer_logits(wfn, net, S, h, feat_prec)
+    sa = cluster_seeds(seeds_from_logits(lg, x0, S, h, thresh[0], 0), cell)
+    tries, used = [], len(sa)
+    ra = wfn.autocritic(sa, prec) if len(sa) else None
+    tries.append({"seeds": len(sa), "ph": None if ra is None else int(ra["ph"])})
+    torch.cuda.synchronize()
+    proposal = {"xyz": ra["xyz"] if ra is not None else np.zeros((0, 3)),
+                "typ": ra["typ"] if ra is not None else np.zeros(0, np.int32),
+                "ph": None if ra is None else int(ra["ph"]), "seeds": len(sa),
+                "ms": 1e3 * (time.perf_counter() - t0)}
+    res = stage = None
+    reason = ""
+    if ra is not None and ra["ph"] == 1:
+        res, stage, reason = ra, "learned", "poincare-hopf"
+    elif ra is not None:
+        sb = cluster_seeds(seeds_from_logits(lg, x0, S, h, thresh[1], 0), cell)
+        used_cells = {tuple(c) for c in np.floor(sa / cell).astype(np.int64)}
+        keep = np.array([tuple(c) not in used_cells for c in np.floor(sb / cell).astype(np.int64)], bool)
+        sb = sb[keep] if len(sb) else sb
+        used += len(sb)
+        rb = wfn.autocritic(sb, prec) if len(sb) else None
+        tries.append({"seeds": len(sb), "ph": None if rb is None else int(rb["ph"])})
+        new = 0
+        if rb is not None:
+            outer = ~core_mask(rb["xyz"], _atoms(wfn))
+            sub = {"xyz": rb["xyz"][outer], "typ": rb["typ"][outer]}
+            new = int((~match_cps(sub, ra, tol=1e-2)).sum())
+        tries[-1]["new_cps"] = new
+        if new == 0:
+            res, stage, reason = ra, "learned", "stable under densification"
+    if res is None:
         res = wfn.autocritic(None, prec)
         used += int(res["nseed"])
-        res["stage"] = "fallback"
+        stage, reason = "fallback", "check failed"
     torch.cuda.synchronize()
     res["ms"] = 1e3 * (time.perf_counter() - t0)
+    res["stage"] = stage
+    res["reason"] = reason
     res["seeds_used"] = used
     res["tries"] = tries
+    res["proposal"] = proposal
     return res
 
 
@@ -308,6 +395,16 @@ def match_cps(ref: dict, got: dict, tol: float = 1e-3) -> np.ndarray:
     return found
 
 
+def compare(ref: dict, got: dict, atom_xyz: np.ndarray) -> dict:
+    """Recall of the plain search's CPs, over all of them and over those
+    outside the nuclear cores."""
+    m = match_cps(ref, got)
+    outer = ~core_mask(ref["xyz"], atom_xyz)
+    return {"recall": float(m.mean()) if len(m) else 1.0,
+            "recall_outside_cores": float(m[outer].mean()) if outer.any() else 1.0,
+            "ncp": int(len(m)), "ncp_outside_cores": int(outer.sum())}
+
+
 # -------------------------------------------------------------- training
 @dataclass
 class Sample:
@@ -318,12 +415,18 @@ class Sample:
     ms_auto: float
 
 
-def make_sample(mol, S: int, h: float, prec: str) -> Sample:
+def make_sample(mol, S: int, h: float, prec: str, label_prec: str = "fp64") -> Sample:
+    """Features and targets of one training molecule.  The targets are the
+    CPs of a non-learned AUTO seeded with critic2's pair seeds plus the
+    coarse-grid minima of s (grid_seeds): on these random-coefficient
+    densities pair seeding alone misses many CPs, and targets that call a
+    real CP "none" would teach the network to suppress it."""
     from .wfn import Wavefunction
     w = Wavefunction(mol)
     try:
         x, x0 = features(w, S, h, prec)
-        res = w.autocritic(None, prec)
+        seeds = np.concatenate([w.pair_seeds(), grid_seeds(w, S, h, prec)])
+        res = w.autocritic(seeds, label_prec)
         lab = cp_labels(res["xyz"], res["typ"], mol.atom_xyz, x0, h, S)
         return Sample(x, lab, mol.natom, len(res["xyz"]), float(res["ms"]))
     finally:
@@ -364,6 +467,46 @@ def train(samples: List[Sample], epochs: int, batch: int, lr: float, S: int, see
     return net
 
 
+def evaluate(mol, net: SeedNet, prec: str = "fp64") -> dict:
+    """Plain AUTO (critic2's pair seeds) against the learned search on one
+    molecule, with the non-learned coarse-grid seeds (minima of s) as the
+    method without the network.  Times are wall times of whole searches."""
+    from .wfn import Wavefunction
+    torch = _torch()
+    w = Wavefunction(mol)
+
+    def timed(f, *a):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = f(*a)
+        torch.cuda.synchronize()
+        return r, 1e3 * (time.perf_counter() - t)
+
+    try:
+        learned_autocritic(w, net, prec)  # warm-up (first-use allocations)
+        ref, ms_plain = timed(w.autocritic, None, prec)
+        got = learned_autocritic(w, net, prec)
+        grid, ms_grid = timed(lambda: w.autocritic(grid_seeds(w), prec))
+        prop = got["proposal"]
+        out = dict(molecule=mol.name, natom=mol.natom, prec=prec, plain_ph=int(ref["ph"]),
+                   plain_seeds=int(ref["nseed"]), ms_plain=round(ms_plain, 1),
+                   learned_ph=int(got["ph"]), stage=got["stage"], reason=got["reason"],
+                   learned_seeds=int(got["seeds_used"]), ms_learned=round(got["ms"], 1),
+                   speedup=round(ms_plain / got["ms"], 2), tries=got["tries"])
+        out.update(compare(ref, got, mol.atom_xyz))
+        c = compare(ref, prop, mol.atom_xyz)
+        out["proposal"] = dict(seeds=prop["seeds"], ms=round(prop["ms"], 1), speedup=round(ms_plain / prop["ms"], 2),
+                               ph=prop["ph"], ncp_found=int(len(prop["xyz"])), recall=c["recall"],
+                               recall_outside_cores=c["recall_outside_cores"])
+        c = compare(ref, grid, mol.atom_xyz)
+        out["grid_seeds"] = dict(seeds=int(grid["nseed"]), ms=round(ms_grid, 1), speedup=round(ms_plain / ms_grid, 2),
+                                 ph=int(grid["ph"]), ncp_found=int(len(grid["xyz"])), recall=c["recall"],
+                                 recall_outside_cores=c["recall_outside_cores"])
+        return out
+    finally:
+        w.close()
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -372,7 +515,8 @@ def main(argv=None):
     t.add_argument("--epochs", type=int, default=12)
     t.add_argument("--batch", type=int, default=4)
     t.add_argument("--lr", type=float, default=2e-3)
-    t.add_argument("--prec", default="tf32x3")
+    t.add_argument("--prec", default="tf32x3", help="precision of the coarse-grid features")
+    t.add_argument("--label-prec", default="fp64", help="precision of the plain AUTO that labels")
     t.add_argument("--nval", type=int, default=8)
     t.add_argument("--out", default=WEIGHTS)
     t.add_argument("--log", default=None)
@@ -390,7 +534,7 @@ def main(argv=None):
         t0 = time.perf_counter()
         samples = []
         for i in range(a.nmol):
-            samples.append(make_sample(synth.training_molecule(i), S, h, a.prec))
+            samples.append(make_sample(synth.training_molecule(i), S, h, a.prec, a.label_prec))
             if (i + 1) % max(1, a.nmol // 20) == 0:
                 log(f"data: {i + 1}/{a.nmol} molecules, {time.perf_counter() - t0:.0f} s, "
                     f"last natom {samples[-1].natom} ncp {samples[-1].ncp} labels {len(samples[-1].labels)}")
@@ -398,23 +542,21 @@ def main(argv=None):
         t1 = time.perf_counter()
         net = train(samples, a.epochs, a.batch, a.lr, S, log=log)
         t_train = time.perf_counter() - t1
-        # held-out check against plain AUTO
-        from .wfn import Wavefunction
+        meta = dict(nmol=a.nmol, epochs=a.epochs, batch=a.batch, lr=a.lr, prec=a.prec, label_prec=a.label_prec,
+                    S=S, h=h, s_data=round(t_data, 1), s_train=round(t_train, 1))
+        net.save(a.out, meta)
+        # held-out check against plain AUTO (FP64 is deterministic; the split
+        # mode finishes every Newton run in FP64)
         rn = net.rounded()
         stats = []
-        for j in range(a.nval):
-            mol = synth.training_molecule(10 ** 6 + j)
-            w = Wavefunction(mol)
-            ref = w.autocritic(None, a.prec)
-            got = learned_autocritic(w, rn, a.prec)
-            rec = match_cps(ref, got)
-            stats.append(dict(natom=mol.natom, ncp=len(ref["xyz"]), recall=float(rec.mean()), ph=int(got["ph"]),
-                              stage=got["stage"], seeds=got["seeds_used"], plain_seeds=int(ref["nseed"]),
-                              ms_plain=float(ref["ms"]), ms_learned=float(got["ms"])))
-            log("val " + json.dumps(stats[-1]))
-            w.close()
-        meta = dict(nmol=a.nmol, epochs=a.epochs, batch=a.batch, lr=a.lr, prec=a.prec, S=S, h=h,
-                    s_data=round(t_data, 1), s_train=round(t_train, 1), val=stats)
+        cases = [(synth.training_molecule(10 ** 6 + j), "fp64") for j in range(a.nval)]
+        cases += [(synth.make_molecule("cp100"), "fp64"), (synth.make_molecule("cp100"), "tf32x3")]
+        for mol, prec in cases:
+            st = evaluate(mol, rn, prec)
+            st["prec"] = prec
+            stats.append(st)
+            log("val " + json.dumps(st))
+        meta["val"] = stats
         net.save(a.out, meta)
         log("saved " + a.out + " " + json.dumps({k: v for k, v in meta.items() if k != "val"}))
     return 0

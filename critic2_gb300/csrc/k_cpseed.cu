@@ -327,32 +327,48 @@ __global__ void k_features(const double *__restrict__ crho, const double *__rest
   *reinterpret_cast<float4 *>(x + 4 * v) = make_float4(f0, f1, f2, 0.f);
 }
 
-// Seeds from the network's output on one S^3 grid: voxels whose largest
-// heat-map logit exceeds thr (and, with local_max, is not exceeded by any of
-// its 26 neighbours; ties go to the lower index), placed at the voxel
-// centre plus the predicted offset (clamped to 1.5 voxels).  Voxel (i,j,k)
-// sits at x0 + h (i, j, k).
+// Seeds from the network's output on one S^3 grid.  mode 0: voxels whose
+// largest heat-map logit exceeds thr; mode 1: ... and whose largest logit is
+// not exceeded by that of any of its 26 neighbours (ties go to the lower
+// index); mode 2: voxels where some CP type's logit exceeds thr and is a
+// maximum of that type's map over the 26 neighbours; mode 3: as 2 over the 6
+// face neighbours.  A seed sits at the voxel centre plus the predicted
+// offset (clamped to 1.5 voxels); voxel (i,j,k) is at x0 + h (i, j, k).
+__device__ __forceinline__ float max4(const float4 &a) { return fmaxf(fmaxf(a.x, a.y), fmaxf(a.z, a.w)); }
+
 __global__ void k_seeds(const float *__restrict__ lg, int S, double x00, double x01, double x02, double h,
-                        float thr, int local_max, int cap, double *__restrict__ seeds, int *__restrict__ vox,
+                        float thr, int mode, int cap, double *__restrict__ seeds, int *__restrict__ vox,
                         int *__restrict__ count) {
   const long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long n = (long)S * S * S;
   if (v >= n) return;
   const float4 a = ld4(lg + 8 * v);
-  const float p = fmaxf(fmaxf(a.x, a.y), fmaxf(a.z, a.w));
+  const float p = max4(a);
   if (!(p > thr)) return;
   const int i = (int)(v / ((long)S * S)), j = (int)((v / S) % S), k = (int)(v % S);
-  if (local_max) {
+  if (mode >= 1) {
+    // per-type candidates: channels above thr (mode >= 2), or the max (mode 1)
+    bool cand[4] = {a.x > thr, a.y > thr, a.z > thr, a.w > thr};
+    const float av[4] = {a.x, a.y, a.z, a.w};
     for (int di = -1; di <= 1; di++)
       for (int dj = -1; dj <= 1; dj++)
         for (int dk = -1; dk <= 1; dk++) {
           const int ii = i + di, jj = j + dj, kk = k + dk;
           if ((di | dj | dk) == 0 || ii < 0 || jj < 0 || kk < 0 || ii >= S || jj >= S || kk >= S) continue;
+          if (mode == 3 && (di != 0) + (dj != 0) + (dk != 0) != 1) continue;
           const long u = ((long)ii * S + jj) * S + kk;
           const float4 b = ld4(lg + 8 * u);
-          const float q = fmaxf(fmaxf(b.x, b.y), fmaxf(b.z, b.w));
-          if (q > p || (q == p && u < v)) return;
+          if (mode == 1) {
+            const float q = max4(b);
+            if (q > p || (q == p && u < v)) return;
+          } else {
+            const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+              if (bv[t] > av[t] || (bv[t] == av[t] && u < v)) cand[t] = false;
+          }
         }
+    if (mode >= 2 && !(cand[0] || cand[1] || cand[2] || cand[3])) return;
   }
   const float4 o = ld4(lg + 8 * v + 4);
   const float oi = fminf(fmaxf(o.x, -1.5f), 1.5f), oj = fminf(fmaxf(o.y, -1.5f), 1.5f),
@@ -514,15 +530,16 @@ int c2g_cs_features(const double *d_crho, const double *d_cgrad, long nvox, floa
   });
 }
 
-int c2g_cs_seeds(const float *logits, int S, const double *x0, double h, float thresh_logit, int local_max,
+int c2g_cs_seeds(const float *logits, int S, const double *x0, double h, float thresh_logit, int mode,
                  int cap, double *d_seeds, int *d_vox, int *d_count, void *stream) {
   return guarded([&] {
     if (!logits || !x0 || !d_seeds || !d_vox || !d_count || S <= 0 || cap < 0) fail(C2G_ERR_ARG, "bad argument");
+    if (mode < 0 || mode > 3) fail(C2G_ERR_ARG, "seed mode must be 0-3");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const long n = (long)S * S * S;
     C2G_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), st));
     k_seeds<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(logits, S, x0[0], x0[1], x0[2], h, thresh_logit,
-                                                         local_max, cap, d_seeds, d_vox, d_count);
+                                                         mode, cap, d_seeds, d_vox, d_count);
     C2G_CUDA(cudaGetLastError());
   });
 }

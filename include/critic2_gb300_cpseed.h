@@ -61,12 +61,14 @@ int c2g_cs_targets(const float *d_cps, int ncp, int S, float *tgt, void *stream)
 int c2g_cs_features(const double *d_crho, const double *d_cgrad, long nvox, float *x, void *stream);
 
 /* Seeds from the network's output on one S^3 grid whose voxel (i,j,k) is
- * at x0 + h*(i,j,k) (x0 a HOST array of 3): voxels whose largest heat-map
- * logit exceeds thresh_logit (with local_max: and is a maximum over its 26
- * neighbours), at the voxel plus the predicted offset.  Writes up to cap
- * seeds d_seeds(3,*) and their voxel indices, *d_count = number found
- * (may exceed cap). */
-int c2g_cs_seeds(const float *logits, int S, const double *x0, double h, float thresh_logit, int local_max,
+ * at x0 + h*(i,j,k) (x0 a HOST array of 3).  mode 0: every voxel whose
+ * largest heat-map logit exceeds thresh_logit; 1: ... that is also a
+ * maximum of the largest logit over its 26 neighbours; 2: voxels where some
+ * CP type's logit exceeds thresh_logit and is a maximum of that type's map
+ * over the 26 neighbours; 3: as 2 over the 6 face neighbours.  A seed is
+ * the voxel plus the predicted offset.  Writes up to cap seeds d_seeds(3,*)
+ * and their voxel indices, *d_count = number found (may exceed cap). */
+int c2g_cs_seeds(const float *logits, int S, const double *x0, double h, float thresh_logit, int mode,
                  int cap, double *d_seeds, int *d_vox, int *d_count, void *stream);
 
 /* One Adam step (bias-corrected, step t >= 1) on n parameters. */
