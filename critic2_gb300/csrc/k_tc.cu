@@ -75,6 +75,11 @@ struct TcKind {
   int kpad = 0;
   PrimTC *prim = nullptr;
   uint8_t *c_hi = nullptr, *c_lo = nullptr;  // [mo_pad][kpad] elements
+  // per-stage cutoff records: stage st owns entries [soff[st], soff[st+1])
+  // = (atom as int bits, largest cutoff, smallest exponent) of each atom
+  // with primitives in the stage
+  int *soff = nullptr;
+  float4 *sent = nullptr;
 };
 
 struct TcOperands {
@@ -138,6 +143,8 @@ struct Mat3 {
 struct TcArgs {
   DevWfn w;
   const PrimTC *prim;
+  const int *soff;
+  const float4 *sent;
   const uint8_t *c_hi, *c_lo;
   const float *occ;
   int nstage, kpad, nmt, maskw;
@@ -690,28 +697,32 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       // in the tile, exp(-min alpha dmin^2); the active stages are listed
       // from the least to the most important one, so that the truncating
       // FP32 accumulators stay small for most of the accumulation.
+      // One lane per stage, from the stage's per-atom records: the atom's
+      // primitive with the smallest exponent has the largest cutoff, so the
+      // stage is active iff that cutoff reaches the tile, and the bound is
+      // that primitive's alpha dmin^2 (the same values as from every
+      // primitive of the stage).
       uint8_t *key = s.key + par * a.maskw * 32;
       uint16_t *list = s.list + par * a.maskw * 32;
-      constexpr int SPB = 32 / KPS;  // stages per ballot
-#pragma unroll 4
-      for (int c0 = 0; c0 < a.maskw * 32; c0 += SPB) {
-        const int k = c0 * KPS + lane;
-        bool act = false;
-        float arg = 3.0e38f;
-        if (nv && k < a.kpad) {
-          const PrimTC pr = a.prim[k];
-          const float dm = fmaxf(dmn[pr.meta >> 12], 0.f);
-          act = pr.dran > 0.f && dmn[pr.meta >> 12] <= pr.dran;
-          if (act) arg = pr.alpha * dm * dm;
+      for (int st0 = 0; st0 < a.maskw * 32; st0 += 32) {
+        const int st = st0 + lane;
+        uint8_t kv = 255;
+        if (nv && st < a.nstage) {
+          bool act = false;
+          float arg = 3.0e38f;
+          const int e1 = a.soff[st + 1];
+          for (int e = a.soff[st]; e < e1; e++) {
+            const float4 E = a.sent[e];
+            const float dmr = dmn[__float_as_int(E.x)];
+            if (dmr <= E.y) {
+              act = true;
+              const float dm = fmaxf(dmr, 0.f);
+              arg = fminf(arg, E.z * dm * dm);
+            }
+          }
+          if (act) kv = (uint8_t)fminf(15.f, arg * 0.5f);
         }
-#pragma unroll
-        for (int o = KPS / 2; o; o >>= 1) arg = fminf(arg, __shfl_xor_sync(0xffffffffu, arg, o));
-        const unsigned b = __ballot_sync(0xffffffffu, act);
-        if ((lane % KPS) == 0) {
-          const int st = c0 + lane / KPS;
-          const bool sact = ((b >> lane) & ((KPS == 32 ? 0u : (1u << KPS)) - 1u)) != 0u;
-          if (st < a.maskw * 32) key[st] = sact ? (uint8_t)fminf(15.f, arg * 0.5f) : (uint8_t)255;
-        }
+        key[st] = kv;
       }
       __syncwarp();
       int nact = 0;
@@ -1096,6 +1107,32 @@ void ensure_kind(Handle &h, int kind) {
     kd.c_lo = reinterpret_cast<uint8_t *>(dev_upload(t, lo));
   }
   kd.prim = dev_upload(t, prim);
+  std::vector<int> soff(kd.nstage + 1, 0);
+  std::vector<float4> sent;
+  for (int st = 0; st < kd.nstage; st++) {
+    soff[st] = (int)sent.size();
+    const size_t first = sent.size();
+    for (int k = st * kd.kps; k < (st + 1) * kd.kps && k < n; k++) {
+      const int at = prim[k].meta >> 12;
+      if (!(prim[k].dran > 0.f)) continue;
+      size_t e = first;
+      while (e < sent.size() && std::memcmp(&sent[e].x, &at, 4) != 0) e++;
+      if (e == sent.size()) {
+        float4 E;
+        std::memcpy(&E.x, &at, 4);
+        E.y = prim[k].dran;
+        E.z = prim[k].alpha;
+        E.w = 0.f;
+        sent.push_back(E);
+      } else {
+        sent[e].y = std::max(sent[e].y, prim[k].dran);
+        sent[e].z = std::min(sent[e].z, prim[k].alpha);
+      }
+    }
+  }
+  soff[kd.nstage] = (int)sent.size();
+  kd.soff = dev_upload(t, soff);
+  kd.sent = dev_upload(t, sent);
   kd.built = true;
 }
 
@@ -1112,6 +1149,8 @@ TcArgs make_args(Handle &h, int kind) {
   TcArgs a{};
   a.w = h.dev;
   a.prim = kd.prim;
+  a.soff = kd.soff;
+  a.sent = kd.sent;
   a.c_hi = kd.c_hi;
   a.c_lo = kd.c_lo;
   a.occ = t->occ;
