@@ -6,17 +6,16 @@
 // followed by the MO reduction of rho2 (src/wfn_private@proc.F90:2546-2624).
 // Here it runs on tcgen05 MMAs with
 //   M = 128 MOs (A = the coefficient tile, resident in tensor memory),
-//   N = (component, point) pairs of half a 32-point tile (B = the basis block
-//       chi built in shared memory, one row per component and point, so one
-//       N = 160 MMA takes all ten components of 16 points),
+//   N = (component, point) pairs of a 32-point tile (B = the basis block chi
+//       built in shared memory, one row per component and point),
 //   K = one 32-byte row of primitives (16 bf16 or 8 tf32),
 // in a 3-product split: A_hi*B_hi + A_hi*B_lo + A_lo*B_hi, FP32 accumulate;
-// per K-step and half-tile five MMAs: hi*hi (N = 160), the two cross
-// products of the value and gradient (N = 64, own accumulator) and of the
-// second derivatives (N = 96, into the main accumulator).  The accumulators
-// (2 x 160 columns for the hi*hi products, 2 x 64 for the cross products
-// of the value and gradient) and 4 coefficient stages (16 columns each)
-// fill the SM's 512 TMEM columns.
+// per K-step six MMAs: hi*hi of components 0-7 (N = 256) and 8-9 (N = 64),
+// the two cross products of the value and gradient (N = 128, own
+// accumulator) and of the second derivatives (N = 192, into the main
+// accumulator).  The accumulators (320 columns for the hi*hi products, 128
+// for the cross products of the value and gradient) and 4 coefficient
+// stages (16 columns each) fill the SM's 512 TMEM columns.
 //
 // CTA roles (persistent, one CTA per SM, 12 warps):
 //   warps 0-3  load the coefficient stage (L2 -> registers -> tcgen05.st into
@@ -99,34 +98,30 @@ namespace K {
 constexpr int NP = 32;     // points per tile
 constexpr int MT = 128;    // MOs per tile (MMA M)
 constexpr int NCOMP = 10;  // value, 3 first, 6 second derivatives
-// The tile's points form two halves of 16; for each half the B operand has
-// one row per (component, point): row = component * 16 + point, so that a
-// single N = 160 MMA covers all ten components of a half (small-N MMAs
-// run at a fraction of the tensor pipe's rate).
-constexpr int NH = 2;                   // point halves per tile
-constexpr int HP = NP / NH;             // 16 points per half
-constexpr int BROWS = NCOMP * HP;       // 160 B rows per half
-constexpr int BPIECE = BROWS * 32;      // 5120 bytes: one (half, hi|lo) B operand
-constexpr int STAGE = NH * 2 * BPIECE;  // bytes of one K-stage (20480)
+// The B operand has one row per (component, point) of the 32-point tile:
+// row = component * 32 + point, 320 rows, so that a K-step takes six MMAs
+// with N = 64-256 (small-N MMAs run at a fraction of the tensor pipe's rate).
+constexpr int BROWS = NCOMP * NP;       // 320 B rows
+constexpr int BPIECE = BROWS * 32;      // 10240 bytes: one (hi|lo) B operand
+constexpr int STAGE = 2 * BPIECE;       // bytes of one K-stage (20480)
 constexpr int NSTAGE = 6;  // shared-memory basis-block stages
 constexpr int NCBUF = 4;   // coefficient buffers in TMEM
 constexpr int NPROD = 6;
 constexpr int W_MMA = 4, W_SETUP = 5, W_PROD0 = 6;
 constexpr int NTHR = (W_PROD0 + NPROD) * 32;  // 384
 constexpr uint32_t TMEM_COLS = 512;
-// TMEM columns: per half, the accumulators of the hi*hi products of the 10
-// components (160 columns, column = component * 16 + point), then per half
-// the accumulators of the cross products (hi*lo + lo*hi) of the value and
-// the gradient (64 columns), then the coefficient buffers.  Keeping the
-// small cross terms apart means the large accumulator takes one truncating
-// addition per MMA step instead of three (the tensor core's FP32
-// accumulation rounds toward zero, so the error grows with the number of
-// additions); the cross terms of the second derivatives go into the main
-// accumulator.
+// TMEM columns: the accumulators of the hi*hi products of the 10 components
+// (320 columns, column = component * 32 + point), the accumulators of the
+// cross products (hi*lo + lo*hi) of the value and the gradient (128
+// columns), then the coefficient buffers.  Keeping the small cross terms
+// apart means the large accumulator takes one truncating addition per MMA
+// step instead of three (the tensor core's FP32 accumulation rounds toward
+// zero, so the error grows with the number of additions); the cross terms
+// of the second derivatives go into the main accumulator.
 constexpr int NXCOMP = 4;
-constexpr int XROWS = NXCOMP * HP;          // 64
-constexpr int XCOL0 = NH * BROWS;           // 320
-constexpr int CBUF0 = XCOL0 + NH * XROWS;   // 448
+constexpr int XROWS = NXCOMP * NP;          // 128
+constexpr int XCOL0 = BROWS;                // 320
+constexpr int CBUF0 = XCOL0 + XROWS;        // 448
 static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
 constexpr uint64_t TIMEOUT_NS = 4000000000ull;
@@ -430,15 +425,14 @@ __device__ __noinline__ void produce_half(const StageRow *rows, int half, const 
       }
     }
   }
-  // point r = half-tile hf, row p; B row of component c = c * 16 + p, whose
-  // 8-row group is 2c + (p >> 3)
-  const int hf = r >> 4, p = r & 15;
-  uint8_t *row = dst + hf * (2 * K::BPIECE) + (p >> 3) * 256 + half * 128 + (p & 7) * 16;
+  // B row of component c at point r = c * 32 + r, whose 8-row group is
+  // 4c + (r >> 3)
+  uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
 #pragma unroll
   for (int c = 0; c < 10; c++)
 #pragma unroll
     for (int pc = 0; pc < 2; pc++)
-      *reinterpret_cast<uint4 *>(row + pc * K::BPIECE + c * 512) =
+      *reinterpret_cast<uint4 *>(row + pc * K::BPIECE + c * 1024) =
           make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
 }
 
@@ -746,8 +740,9 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
     // ------------------------------------------------------------ MMA issue
     if (lane == 0) {
       constexpr uint32_t fmt = KIND == 0 ? 1 : 2;
-      constexpr uint32_t id_all = ptx::make_idesc(fmt, K::MT, K::BROWS);           // 10 components
-      constexpr uint32_t id_x = ptx::make_idesc(fmt, K::MT, K::XROWS);             // components 0-3
+      constexpr uint32_t id_256 = ptx::make_idesc(fmt, K::MT, 256);  // components 0-7
+      constexpr uint32_t id_64 = ptx::make_idesc(fmt, K::MT, 64);    // components 8-9
+      constexpr uint32_t id_x = ptx::make_idesc(fmt, K::MT, K::XROWS);            // components 0-3
       constexpr uint32_t id_h = ptx::make_idesc(fmt, K::MT, K::BROWS - K::XROWS);  // components 4-9
       uint32_t g = 0, u = 0;
       bool ok = true;
@@ -768,28 +763,31 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
             const uint32_t a_hi = tmem + K::CBUF0 + cb * 16, a_lo = a_hi + 8;
             const uint32_t sb = ptx::smem_u32(s.stage + b * K::STAGE);
             const uint32_t acc0 = j > 0 ? 1u : 0u;
-#pragma unroll
-            for (int hf = 0; hf < K::NH; hf++) {
-              const uint32_t dcol = tmem + hf * K::BROWS, xcol = tmem + K::XCOL0 + hf * K::XROWS;
-              const uint32_t sh = sb + hf * 2 * K::BPIECE, sl = sh + K::BPIECE;
+            {
+              const uint32_t sh = sb, sl = sb + K::BPIECE;
+              const uint32_t dcol = tmem, xcol = tmem + K::XCOL0;
               const uint64_t bh = ptx::smem_desc_kmajor(sh, 128, 256);
               const uint64_t bl = ptx::smem_desc_kmajor(sl, 128, 256);
-              // rows 64-159 (components 4-9) start 8 row groups in
-              const uint64_t bh2 = ptx::smem_desc_kmajor(sh + 8 * 256, 128, 256);
-              const uint64_t bl2 = ptx::smem_desc_kmajor(sl + 8 * 256, 128, 256);
-              const uint32_t dcol2 = dcol + K::XROWS;
+              // rows 256-319 (components 8-9) start 32 row groups in, rows
+              // 128-319 (components 4-9) 16 row groups in
+              const uint64_t bh8 = ptx::smem_desc_kmajor(sh + 32 * 256, 128, 256);
+              const uint64_t bh4 = ptx::smem_desc_kmajor(sh + 16 * 256, 128, 256);
+              const uint64_t bl4 = ptx::smem_desc_kmajor(sl + 16 * 256, 128, 256);
+              const uint32_t d8 = dcol + 256, d4 = dcol + K::XROWS;
               if constexpr (KIND == 0) {
-                ptx::mma_bf16_ts(dcol, a_hi, bh, id_all, acc0);
+                ptx::mma_bf16_ts(dcol, a_hi, bh, id_256, acc0);
+                ptx::mma_bf16_ts(d8, a_hi, bh8, id_64, acc0);
                 ptx::mma_bf16_ts(xcol, a_hi, bl, id_x, acc0);
                 ptx::mma_bf16_ts(xcol, a_lo, bh, id_x, 1u);
-                ptx::mma_bf16_ts(dcol2, a_hi, bl2, id_h, 1u);
-                ptx::mma_bf16_ts(dcol2, a_lo, bh2, id_h, 1u);
+                ptx::mma_bf16_ts(d4, a_hi, bl4, id_h, 1u);
+                ptx::mma_bf16_ts(d4, a_lo, bh4, id_h, 1u);
               } else {
-                ptx::mma_tf32_ts(dcol, a_hi, bh, id_all, acc0);
+                ptx::mma_tf32_ts(dcol, a_hi, bh, id_256, acc0);
+                ptx::mma_tf32_ts(d8, a_hi, bh8, id_64, acc0);
                 ptx::mma_tf32_ts(xcol, a_hi, bl, id_x, acc0);
                 ptx::mma_tf32_ts(xcol, a_lo, bh, id_x, 1u);
-                ptx::mma_tf32_ts(dcol2, a_hi, bl2, id_h, 1u);
-                ptx::mma_tf32_ts(dcol2, a_lo, bh2, id_h, 1u);
+                ptx::mma_tf32_ts(d4, a_hi, bl4, id_h, 1u);
+                ptx::mma_tf32_ts(d4, a_lo, bh4, id_h, 1u);
               }
             }
             ptx::mma_commit(&s.bar[K::B_EMPTY + b]);
@@ -884,13 +882,13 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
 #pragma unroll 1
           for (int ch = 0; ch < 4; ch++) {
             uint32_t v[10][8], xv[K::NXCOMP][8];
-            // points ch*8 .. ch*8+7: half ch/2, rows (ch%2)*8 ..
-            const uint32_t dc = tmem + lanebase + (ch >> 1) * K::BROWS + (ch & 1) * 8;
-            const uint32_t xc = tmem + lanebase + K::XCOL0 + (ch >> 1) * K::XROWS + (ch & 1) * 8;
+            // points ch*8 .. ch*8+7
+            const uint32_t dc = tmem + lanebase + ch * 8;
+            const uint32_t xc = tmem + lanebase + K::XCOL0 + ch * 8;
 #pragma unroll
-            for (int c = 0; c < 10; c++) ptx::tmem_ld8(dc + c * K::HP, v[c]);
+            for (int c = 0; c < 10; c++) ptx::tmem_ld8(dc + c * K::NP, v[c]);
 #pragma unroll
-            for (int c = 0; c < K::NXCOMP; c++) ptx::tmem_ld8(xc + c * K::HP, xv[c]);
+            for (int c = 0; c < K::NXCOMP; c++) ptx::tmem_ld8(xc + c * K::NP, xv[c]);
             ptx::tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 8; j++) {
