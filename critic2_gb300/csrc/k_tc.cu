@@ -124,6 +124,7 @@ constexpr int XCOL0 = BROWS;                // 320
 constexpr int CBUF0 = XCOL0 + XROWS;        // 448
 static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
+constexpr int TAB = 4 * 13;  // axis-factor table: 4 primitives x (1 x + 4 y + 8 z values)
 constexpr uint64_t TIMEOUT_NS = 4000000000ull;
 // barrier slots
 constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17, B_EPIFULL = 18,
@@ -168,6 +169,8 @@ struct Smem {
   float4 *offl;  // [2][natom] (o - o_hi, |o|^2 - |o|^2_hi)
   float *dmin;   // [2][natom] lower bound of the tile-atom distance
   StageRow *rows;  // [NPROD][16] stage primitive data of each producer warp
+  float4 *tab;     // [NPROD][52] axis-factor tables of the brick path
+  int *brick;      // [2] tile is a separable brick (see the setup warp)
 };
 
 __host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs) {
@@ -192,12 +195,13 @@ __host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs)
   offs[11] = take((size_t)2 * natom * 16, 16);
   offs[12] = take((size_t)2 * natom * 4, 16);
   offs[13] = take((size_t)K::NPROD * 16 * sizeof(StageRow), 16);
+  offs[14] = take((size_t)K::NPROD * K::TAB * sizeof(float4), 16);
   return o + 1024;  // slack for aligning the dynamic base
 }
 
 __device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
   uint8_t *base = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
-  size_t o[14];
+  size_t o[15];
   smem_bytes(natom, maskw, o);
   Smem s;
   s.stage = base + o[0];
@@ -218,6 +222,8 @@ __device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
   s.offl = (float4 *)(base + o[11]);
   s.dmin = (float *)(base + o[12]);
   s.rows = (StageRow *)(base + o[13]);
+  s.tab = (float4 *)(base + o[14]);
+  s.brick = (int *)(base + o[8] + 24);
   return s;
 }
 
@@ -436,11 +442,102 @@ __device__ __noinline__ void produce_half(const StageRow *rows, int half, const 
           make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
 }
 
+// Brick form of produce_half: per group of 4 primitives, the warp first
+// tabulates the three Cartesian factors (f0, f1, f2 of the axis, and the
+// axis's share of the exponent argument) for the tile's 1 x, 4 y and 8 z
+// offsets, then every lane forms chi from the three entries of its point.
+// The factors and the per-primitive data are the ones of chi10.
+template <int KIND, bool ANYL>
+__device__ __noinline__ void produce_half_brick(const StageRow *rows, int half, const PointD &d, uint8_t *dst,
+                                                float4 *tab, const float4 *dlt) {
+  constexpr int PPB = KIND == 0 ? 8 : 4;
+  const int r = threadIdx.x & 31;
+  const int jo = r >> 3, ko = r & 7;
+  uint32_t wv[10][2][4];
+#pragma unroll
+  for (int g0 = 0; g0 < PPB; g0 += 4) {
+    __syncwarp();
+    for (int e = r; e < K::TAB; e += 32) {
+      const int jp = e / 13, w = e - 13 * jp;
+      const int j = half * PPB + g0 + jp;
+      const float4 o = rows[j].o, l = rows[j].l, c = rows[j].c;
+      const int lp = __float_as_int(c.z);
+      const bool direct = __float_as_int(c.w) != 0;
+      float oa, la, dd;
+      int lax;
+      if (w == 0) {
+        oa = o.x, la = l.x, dd = dlt[0].x, lax = lp & 15;
+      } else if (w < 5) {
+        oa = o.y, la = l.y, dd = dlt[(w - 1) * 8].y, lax = (lp >> 4) & 15;
+      } else {
+        oa = o.z, la = l.z, dd = dlt[w - 5].z, lax = (lp >> 8) & 15;
+      }
+      const float da = (oa + dd) + la;
+      const float arg = direct ? da * da : fmaf(oa, 2.f * dd, dd * dd);
+      float f0, f1, f2;
+      if constexpr (ANYL) axis_any(da, lax, -2.f * c.y, f0, f1, f2);
+      else axis_f(da, lax, -2.f * c.y, f0, f1, f2);
+      tab[e] = make_float4(f0, f1, f2, arg);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int jp = 0; jp < 4; jp += (KIND == 0 ? 2 : 1)) {
+      float cc[2][10];
+#pragma unroll
+      for (int q = 0; q < (KIND == 0 ? 2 : 1); q++) {
+        const int j = half * PPB + g0 + jp + q;
+        const float4 X = tab[(jp + q) * 13], Y = tab[(jp + q) * 13 + 1 + jo], Z = tab[(jp + q) * 13 + 5 + ko];
+        const float4 o = rows[j].o, l = rows[j].l, c = rows[j].c;
+        const float targ = (X.w + Y.w) + Z.w;
+        const bool in = d.valid && (targ <= l.w);
+        const float ex = in ? o.w * exp2f(-c.x * targ) : 0.f;
+        const float yz = Y.x * Z.x * ex, xz = X.x * Z.x * ex, xy = X.x * Y.x * ex;
+        cc[q][0] = X.x * yz;
+        cc[q][1] = X.y * yz;
+        cc[q][2] = Y.y * xz;
+        cc[q][3] = Z.y * xy;
+        cc[q][4] = X.z * yz;
+        cc[q][5] = Y.z * xz;
+        cc[q][6] = Z.z * xy;
+        const float x1e = X.y * ex;
+        cc[q][7] = x1e * Y.y * Z.x;
+        cc[q][8] = x1e * Z.y * Y.x;
+        cc[q][9] = Y.y * Z.y * X.x * ex;
+      }
+      const int wd = (g0 + jp) >> (KIND == 0 ? 1 : 0);
+      if constexpr (KIND == 0) {
+#pragma unroll
+        for (int c = 0; c < 10; c++) {
+          const __nv_bfloat162 hi = __floats2bfloat162_rn(cc[0][c], cc[1][c]);
+          const float2 hf = __bfloat1622float2(hi);
+          const __nv_bfloat162 lo = __floats2bfloat162_rn(cc[0][c] - hf.x, cc[1][c] - hf.y);
+          wv[c][0][wd] = *reinterpret_cast<const uint32_t *>(&hi);
+          wv[c][1][wd] = *reinterpret_cast<const uint32_t *>(&lo);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 10; c++) {
+          const uint32_t hi = tf32_rna(cc[0][c]);
+          wv[c][0][wd] = hi;
+          wv[c][1][wd] = tf32_rna(cc[0][c] - __uint_as_float(hi));
+        }
+      }
+    }
+  }
+  uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
+#pragma unroll
+  for (int c = 0; c < 10; c++)
+#pragma unroll
+    for (int pc = 0; pc < 2; pc++)
+      *reinterpret_cast<uint4 *>(row + pc * K::BPIECE + c * 1024) =
+          make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
+}
+
 // Builds one K-stage of the basis block (lane = point row).  The stage's
 // primitive data is loaded once (lane j holds primitive j) and broadcast.
 template <int KIND>
 __device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
-                                        const PointD &d, float rad, StageRow *rows) {
+                                        const PointD &d, float rad, StageRow *rows, float4 *tab) {
   constexpr int KPS = KIND == 0 ? 16 : 8;
   const int r = threadIdx.x & 31;
   int lmax = 0;
@@ -454,9 +551,17 @@ __device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par,
     lmax = max(q.lp & 15, max((q.lp >> 4) & 15, (q.lp >> 8) & 15));
   }
   lmax = __reduce_max_sync(0xffffffffu, lmax);  // also orders the row writes before the reads
-  for (int half = 0; half < 2; half++) {
-    if (lmax <= 3) produce_half<KIND, false>(rows, half, d, dst);
-    else produce_half<KIND, true>(rows, half, d, dst);
+  if (s.brick[par]) {
+    const float4 *dlt = s.dl + par * 32;
+    for (int half = 0; half < 2; half++) {
+      if (lmax <= 3) produce_half_brick<KIND, false>(rows, half, d, dst, tab, dlt);
+      else produce_half_brick<KIND, true>(rows, half, d, dst, tab, dlt);
+    }
+  } else {
+    for (int half = 0; half < 2; half++) {
+      if (lmax <= 3) produce_half<KIND, false>(rows, half, d, dst);
+      else produce_half<KIND, true>(rows, half, d, dst);
+    }
   }
   __syncwarp();
 }
@@ -670,6 +775,18 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       const float4 dl = v ? make_float4((float)(x[0] - ref[0]), (float)(x[1] - ref[1]), (float)(x[2] - ref[2]), 1.f)
                           : make_float4(0.f, 0.f, 0.f, 0.f);
       s.dl[par * 32 + lane] = dl;
+      // Separable brick: every valid point's offset is (x offset of lane 0,
+      // y offset of lane 8*(lane/8), z offset of lane lane%8), as for the
+      // 1 x 4 x 8 grid tiles of an axis-aligned grid.  Then each Cartesian
+      // factor of a primitive takes 1, 4 and 8 distinct values in the tile.
+      {
+        const float bx = __shfl_sync(0xffffffffu, dl.x, 0);
+        const float by = __shfl_sync(0xffffffffu, dl.y, lane & 24);
+        const float bz = __shfl_sync(0xffffffffu, dl.z, lane & 7);
+        const bool okb = !v || (dl.x == bx && dl.y == by && dl.z == bz);
+        const bool br = __all_sync(0xffffffffu, okb);
+        if (lane == 0) s.brick[par] = br ? 1 : 0;
+      }
       float rad = v ? sqrtf(dl.x * dl.x + dl.y * dl.y + dl.z * dl.z) : 0.f;
       for (int o = 16; o; o >>= 1) rad = fmaxf(rad, __shfl_xor_sync(0xffffffffu, rad, o));
       float4 *off = s.off + par * a.w.natom;
@@ -825,7 +942,8 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           const int b = g % K::NSTAGE;
           if (g >= (uint32_t)K::NSTAGE && !(ok = warp_wait(s, K::B_EMPTY + b, ((g / K::NSTAGE) - 1) & 1, a.err)))
             break;
-          produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, rad, s.rows + pw * 16);
+          produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, rad, s.rows + pw * 16,
+                        s.tab + pw * K::TAB);
           ptx::fence_proxy_async_smem();
           __syncwarp();
           if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_CHI + b]);
@@ -1177,7 +1295,7 @@ int sm_count() {
 template <int KIND, class Src, class Sink>
 void launch_tc(const TcArgs &a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st) {
   if (ntiles <= 0) return;
-  size_t offs[14];
+  size_t offs[15];
   const size_t bytes = smem_bytes(a.w.natom, a.maskw, offs);
   if (bytes > 227 * 1024) fail(C2G_ERR_UNSUPPORTED, "molecule too large for the split-precision kernel's shared memory");
   auto fn = k_tc<KIND, Src, Sink>;
