@@ -199,6 +199,7 @@ def main():
     ap.add_argument("--grid", type=int, default=0, help="grid points per axis (default: the workload's)")
     ap.add_argument("--binned", action="store_true", help="FP64 comparison binned by rho decade")
     ap.add_argument("--no-cp", action="store_true", help="skip the CP-search part")
+    ap.add_argument("--no-files", action="store_true", help="skip the cube/dat output part")
     ap.add_argument("--fp64-planes", type=int, default=0, help="FP64 comparison on this many i-planes")
     ap.add_argument("--cp-prec", default="fp64,tf32x3")
     args = ap.parse_args()
@@ -355,6 +356,16 @@ def main():
             "fp64_recheck_points": nrecheck}
     if fp64:
         line["fp64_plain"] = fp64
+    if rank == 0 and not args.no_files:
+        # nciplot end to end into files: the cutoff pass and the cube/dat
+        # text (critic2's output step), timed by parts
+        with tempfile.TemporaryDirectory() as d:
+            root = os.path.join(d, "nci")
+            _, parts = w.nciplot_files(x0, xm, ns, prec, root)
+            sizes = {k: os.path.getsize(root + k) for k in ("-dens.cube", "-grad.cube", ".dat")}
+        line["nci_files"] = {"ms_evaluation": parts[0], "ms_cutoff_pass": parts[1], "ms_text": parts[2],
+                             "ms_write": parts[3], "bytes": sizes,
+                             "note": "text formatted on the GPU (correctly rounded, near ties on the host)"}
     if rank == 0 and not args.no_cp:
         cps = cp_search(args)
         if cps:

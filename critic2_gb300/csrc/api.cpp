@@ -9,6 +9,7 @@
 #include <string>
 
 #include "c2g_internal.h"
+#include "k_cube.h"
 #include "k_tc.h"
 
 namespace c2g {
@@ -536,6 +537,160 @@ int c2g_nciplot(c2g_wfn *hp, const double *x0, const double *xmat, const int *ns
     if (rc != C2G_OK) fail(rc, g_last_error);
     C2G_CUDA(cudaMemcpy(crho, dr.p, sizeof(double) * np, cudaMemcpyDeviceToHost));
     C2G_CUDA(cudaMemcpy(cgrad, dg.p, sizeof(double) * np, cudaMemcpyDeviceToHost));
+  });
+}
+
+}  // extern "C"
+
+namespace {
+
+c2g::NciCut to_cut(const c2g_nci_cut *c) {
+  c2g::NciCut k;
+  if (c) {
+    k.rhocut = c->rhocut, k.dimcut = c->dimcut, k.rhoplot = c->rhoplot;
+    k.srho_lo = c->srho_lo, k.srho_hi = c->srho_hi, k.onlyneg = c->onlyneg;
+  } else {
+    // critic2's defaults for a density field (src/nci@proc.f90:141-168)
+    k.rhocut = 0.2, k.dimcut = 2.0, k.rhoplot = 0.1, k.srho_lo = -1e30, k.srho_hi = 1e30, k.onlyneg = 0;
+  }
+  return k;
+}
+
+void put_cube_header(std::string &o, const char *l1, const char *l2, const HostWfn &w, const double *x0,
+                     const double *xmat, const int *nstep) {
+  // src/nci@proc.f90:818-914 for a molecule without fragments: the atoms
+  // inside the cube (0.1 bohr margin), or all atoms when none is inside
+  char b[160];
+  double x1[3];
+  for (int c = 0; c < 3; c++)
+    x1[c] = x0[c] + (nstep[0] - 1) * xmat[c] + (nstep[1] - 1) * xmat[3 + c] + (nstep[2] - 1) * xmat[6 + c];
+  std::vector<int> in;
+  for (int a = 0; a < w.natom; a++) {
+    bool ok = true;
+    for (int c = 0; c < 3; c++) {
+      const double lo = std::min(x0[c], x1[c]) - 0.1, hi = std::max(x0[c], x1[c]) + 0.1;
+      ok = ok && w.xyz[3 * a + c] > lo && w.xyz[3 * a + c] < hi;
+    }
+    if (ok) in.push_back(a);
+  }
+  if (in.empty())
+    for (int a = 0; a < w.natom; a++) in.push_back(a);
+  o += " ";
+  o += l1;
+  o += "\n ";
+  o += l2;
+  o += "\n";
+  std::snprintf(b, sizeof b, "%5d%12.6f%12.6f%12.6f\n", (int)in.size(), x0[0], x0[1], x0[2]);
+  o += b;
+  for (int c = 0; c < 3; c++) {
+    std::snprintf(b, sizeof b, "%5d%12.6f%12.6f%12.6f\n", nstep[c], xmat[3 * c], xmat[3 * c + 1], xmat[3 * c + 2]);
+    o += b;
+  }
+  for (int a : in) {
+    std::snprintf(b, sizeof b, "%4d%5.1f%11.6f%11.6f%11.6f\n", w.z[a], 0.0, w.xyz[3 * a], w.xyz[3 * a + 1],
+                  w.xyz[3 * a + 2]);
+    o += b;
+  }
+}
+
+void write_file(const std::string &path, const std::string &head, const char *body, size_t nbody) {
+  FILE *f = std::fopen(path.c_str(), "wb");
+  if (!f) fail(C2G_ERR_IO, "cannot open " + path + " for writing");
+  const bool ok = std::fwrite(head.data(), 1, head.size(), f) == head.size() &&
+                  (nbody == 0 || std::fwrite(body, 1, nbody, f) == nbody);
+  if (std::fclose(f) != 0 || !ok) fail(C2G_ERR_IO, "write failed: " + path);
+}
+
+double ms_since(std::chrono::steady_clock::time_point t) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+int c2g_nci_post_dev(const int *nstep, const double *d_crho, double *d_cgrad, const c2g_nci_cut *cut,
+                     double *d_dat, long cap, long *ndat, void *stream) {
+  return guarded([&] {
+    require(nstep && d_crho && d_cgrad && ndat && (cap == 0 || d_dat), "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    const long n = (long)nstep[0] * nstep[1] * nstep[2];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DevBuf bc(sizeof(int) * ((n + 255) / 256)), tot(sizeof(long));
+    *ndat = nci_post_dev(nstep, d_crho, d_cgrad, to_cut(cut), d_dat, cap, bc.as<int>(), tot.as<long>(), st);
+  });
+}
+
+int c2g_cube_text(const int *nstep, const double *d_values, char *text, long cap, long *nbytes, void *stream) {
+  return guarded([&] {
+    require(nstep && d_values && nbytes, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    const long nb = cube_body_bytes(nstep);
+    *nbytes = nb;
+    if (!text) return;
+    if (cap < nb) fail(C2G_ERR_ARG, "text buffer too small (" + std::to_string(nb) + " bytes needed)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DevBuf dt(nb), sc(sizeof(int) * cube_flag_scratch_ints());
+    cube_text_dev(nstep, d_values, dt.as<char>(), text, sc.as<int>(), st);
+  });
+}
+
+int c2g_dat_text(const double *d_dat, long ndat, char *text, long cap, long *nbytes, void *stream) {
+  return guarded([&] {
+    require(ndat >= 0 && nbytes && (ndat == 0 || d_dat), "bad argument");
+    const long nb = 31 * ndat;
+    *nbytes = nb;
+    if (!text || ndat == 0) return;
+    if (cap < nb) fail(C2G_ERR_ARG, "text buffer too small (" + std::to_string(nb) + " bytes needed)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DevBuf dt(nb), sc(sizeof(int) * cube_flag_scratch_ints());
+    dat_text_dev(d_dat, ndat, dt.as<char>(), text, sc.as<int>(), st);
+  });
+}
+
+int c2g_nciplot_files(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec,
+                      const char *root, const c2g_nci_cut *cut, c2g_nci_stats *stats, double *ms_parts) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(x0 && xmat && nstep && root, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    DeviceGuard g(h->device);
+    const long n = (long)nstep[0] * nstep[1] * nstep[2];
+    auto t0 = std::chrono::steady_clock::now();
+    DevBuf dr(sizeof(double) * n), dg(sizeof(double) * n);
+    int rc = c2g_nciplot_dev(hp, x0, xmat, nstep, prec, dr.as<double>(), dg.as<double>(), nullptr, stats);
+    if (rc != C2G_OK) fail(rc, g_last_error);
+    C2G_CUDA(cudaDeviceSynchronize());
+    const double t_eval = ms_since(t0);
+    auto t1 = std::chrono::steady_clock::now();
+    DevBuf dd(sizeof(double) * 2 * n), bc(sizeof(int) * ((n + 255) / 256)), tot(sizeof(long));
+    const long ndat = nci_post_dev(nstep, dr.as<double>(), dg.as<double>(), to_cut(cut), dd.as<double>(), n,
+                                   bc.as<int>(), tot.as<long>(), nullptr);
+    const double t_post = ms_since(t1);
+    auto t2 = std::chrono::steady_clock::now();
+    const long nb = cube_body_bytes(nstep);
+    std::vector<char> hd(nb), hg(nb), ht((size_t)std::max(1L, 31 * ndat));
+    {
+      DevBuf dt(std::max(nb, 31 * ndat)), sc(sizeof(int) * cube_flag_scratch_ints());
+      cube_text_dev(nstep, dr.as<double>(), dt.as<char>(), hd.data(), sc.as<int>(), nullptr);
+      cube_text_dev(nstep, dg.as<double>(), dt.as<char>(), hg.data(), sc.as<int>(), nullptr);
+      dat_text_dev(dd.as<double>(), ndat, dt.as<char>(), ht.data(), sc.as<int>(), nullptr);
+    }
+    const double t_fmt = ms_since(t2);
+    auto t3 = std::chrono::steady_clock::now();
+    std::string hdens, hgrad;
+    put_cube_header(hdens, "dens_cube", "3d plot, density", h->host, x0, xmat, nstep);
+    put_cube_header(hgrad, "grad_cube", "3d plot, reduced density gradient", h->host, x0, xmat, nstep);
+    const std::string r(root);
+    write_file(r + "-dens.cube", hdens, hd.data(), nb);
+    write_file(r + "-grad.cube", hgrad, hg.data(), nb);
+    write_file(r + ".dat", std::string(), ht.data(), (size_t)(31 * ndat));
+    if (ms_parts) {
+      ms_parts[0] = t_eval;
+      ms_parts[1] = t_post;
+      ms_parts[2] = t_fmt;
+      ms_parts[3] = ms_since(t3);
+    }
   });
 }
 

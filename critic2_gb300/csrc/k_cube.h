@@ -1,0 +1,42 @@
+// NCI post-pass and cube/dat text (k_cube.cu): internal interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "c2g_internal.h"
+
+namespace c2g {
+
+// critic2's nciplot cutoffs (src/nci@proc.f90:141-168, 612-645)
+struct NciCut {
+  double rhocut, dimcut, rhoplot, srho_lo, srho_hi;
+  int onlyneg;
+};
+
+// Host formatters of the Fortran edit descriptors (correctly rounded):
+// " " + 1p,e13.5e3 (14 characters) and 1p,E15.7 (15 characters).
+void fmt_e13_5e3(double x, char *out);
+void fmt_E15_7(double x, char *out);
+
+// Bytes of a cube record of n3 numbers and of a whole cube body.
+long cube_record_bytes(int n3);
+long cube_body_bytes(const int *nstep);
+
+// Ints of device scratch the text functions need.
+int cube_flag_scratch_ints();
+
+// Cube body of d_v (k fastest) into d_text; copied to h_text (and fixed up
+// there) when h_text is not null, else fixed up on the device.
+void cube_text_dev(const int *nstep, const double *d_v, char *d_text, char *h_text, int *d_scratch,
+                   cudaStream_t st);
+
+// dat lines (31 bytes each) of ndat (crho/100, s) pairs.
+void dat_text_dev(const double *d_dat, long ndat, char *d_text, char *h_text, int *d_scratch, cudaStream_t st);
+
+// Post-pass: writes up to cap dat pairs into d_dat in grid order, applies
+// the s := 100 rules to d_cgrad, returns the number of dat pairs.
+// d_bcount: (npoints + 255) / 256 ints; d_total: one long.
+long nci_post_dev(const int *nstep, const double *d_crho, double *d_cgrad, const NciCut &cut, double *d_dat,
+                  long cap, int *d_bcount, long *d_total, cudaStream_t st);
+
+}  // namespace c2g

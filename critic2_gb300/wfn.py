@@ -141,6 +141,23 @@ class Wavefunction:
                                                 C.c_void_p(d_crho), C.c_void_p(d_cgrad),
                                                 C.c_void_p(stream)))
 
+    def nciplot_files(self, x0, xmat, nstep, prec, root: str, cut=None):
+        """nciplot end to end into root-dens.cube, root-grad.cube and
+        root.dat (c2g_nciplot_files).  cut: None (critic2's defaults) or a
+        dict of rhocut, dimcut, rhoplot, srho_lo, srho_hi, onlyneg.  Returns
+        (stats, ms) with ms = evaluation, cutoff pass, formatting, writes."""
+        st = L.NciStats()
+        ms = np.zeros(4)
+        c = None
+        if cut is not None:
+            d = dict(rhocut=0.2, dimcut=2.0, rhoplot=0.1, srho_lo=-1e30, srho_hi=1e30, onlyneg=0)
+            d.update(cut)
+            c = L.NciCut(**{k: (int(v) if k == "onlyneg" else float(v)) for k, v in d.items()})
+        xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+        L.check(L.lib().c2g_nciplot_files(self._h, _f64(x0), xm, _i32(nstep), _prec(prec), root.encode(),
+                                          C.byref(c) if c is not None else None, C.byref(st), ms))
+        return st, ms
+
     # -------------------------------------------------------------- Newton
     def newton(self, xyz, gfnormeps: float = 1e-12, maxit: int = 200, prec="fp64"):
         x = _f64(xyz).reshape(-1, 3).copy()

@@ -181,6 +181,42 @@ int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int 
 int c2g_nciplot_dev_noalloc(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep,
                             int prec, double *d_crho, double *d_cgrad, void *stream);
 
+/* NCI post-pass cutoffs (src/nci@proc.f90:141-168): .dat gets the points
+ * with |rho| < rhocut and s < dimcut; then s := 100 where |rho| > rhoplot,
+ * where sign(lambda2)*rho is outside [srho_lo, srho_hi], or (onlyneg) where
+ * it is positive.  A NULL cut means critic2's defaults for a density field:
+ * 0.2, 2.0, 0.1, -1e30, 1e30, 0. */
+typedef struct {
+  double rhocut, dimcut, rhoplot, srho_lo, srho_hi;
+  int onlyneg;
+} c2g_nci_cut;
+
+/* The cutoff pass of nciplot (src/nci@proc.f90:612-645, no fragments, no
+ * void) on device cubes in (k,j,i) order: writes the .dat pairs
+ * (sign(lambda2)*rho, s) of the selected points in grid order into
+ * d_dat(2, cap) (up to cap pairs), sets *ndat to their number, and applies
+ * the s := 100 rules to d_cgrad in place. */
+int c2g_nci_post_dev(const int *nstep, const double *d_crho, double *d_cgrad, const c2g_nci_cut *cut,
+                     double *d_dat, long cap, long *ndat, void *stream);
+
+/* write_cube_body (src/nci@proc.f90:916-932) of a device cube in (k,j,i)
+ * order into the host buffer text: records of nstep(3) numbers in
+ * Fortran's (6(" ",1p,e13.5e3)) layout.  *nbytes = size of the text; with
+ * text NULL only *nbytes is set.  Formatted on the GPU, correctly rounded. */
+int c2g_cube_text(const int *nstep, const double *d_values, char *text, long cap, long *nbytes, void *stream);
+
+/* The .dat lines (1p,E15.7,E15.7; src/nci@proc.f90:638) of ndat device
+ * pairs d_dat(2, ndat) into the host buffer text (31 bytes a line). */
+int c2g_dat_text(const double *d_dat, long ndat, char *text, long cap, long *nbytes, void *stream);
+
+/* nciplot end to end: the grid (c2g_nciplot), the cutoff pass and the
+ * files root-dens.cube, root-grad.cube (headers as write_cube_header,
+ * src/nci@proc.f90:818-914, atoms in the frame of the handle) and root.dat.
+ * ms_parts (may be NULL) receives 4 wall times in ms: evaluation, cutoff
+ * pass, text formatting (device) + copies, file writes. */
+int c2g_nciplot_files(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec,
+                      const char *root, const c2g_nci_cut *cut, c2g_nci_stats *stats, double *ms_parts);
+
 /* field%newton for n seeds at once (src/fieldmod@proc.f90:2238-2279):
  * xyz(3,n) in/out; ier(n): 0 converged (|grad| < gfnormeps), 1 invalid or
  * singular Hessian, 2 maxit reached.  In the split modes the iterations run

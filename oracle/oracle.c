@@ -8,6 +8,7 @@
 #include "oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -722,4 +723,66 @@ int o_autocritic(const owfn *w, int nseed, const double *xseed, int nthreads, in
   free(ier);
   free(cps);
   return ncp;
+}
+
+/* ------------------------------------------------------------ NCI output */
+/* Fortran list output of (" ",1p,e13.5e3): blank, then the number right-
+ * justified in 13 columns with 6 significant digits and a 3-digit
+ * exponent (the C library's conversion is correctly rounded). */
+void o_fmt_e13_5e3(double x, char *out) {
+  char buf[64], t[96];
+  snprintf(buf, sizeof buf, "%.5E", x);
+  char *p = strchr(buf, 'E');
+  int e = atoi(p + 1);
+  *p = 0;
+  snprintf(t, sizeof t, " %8sE%c%03d", buf, e < 0 ? '-' : '+', e < 0 ? -e : e);
+  memcpy(out, t, 14);
+}
+
+/* 1p,E15.7: 8 significant digits right-justified in 15 columns; an
+ * exponent beyond +-99 is written as sign and three digits, without E. */
+void o_fmt_E15_7(double x, char *out) {
+  char buf[64], t[96];
+  snprintf(buf, sizeof buf, "%.7E", x);
+  char *p = strchr(buf, 'E');
+  int e = atoi(p + 1);
+  *p = 0;
+  int ae = e < 0 ? -e : e;
+  if (ae > 99) snprintf(t, sizeof t, "%11s%c%03d", buf, e < 0 ? '-' : '+', ae);
+  else snprintf(t, sizeof t, "%11sE%c%02d", buf, e < 0 ? '-' : '+', ae);
+  memcpy(out, t, 15);
+}
+
+/* write_cube_body: do i; do j; write (lu,'(6(" ",1p,e13.5e3))') c(:,j,i)
+ * (src/nci@proc.f90:916-932) */
+long o_cube_body(const int nstep[3], const double *v, char *out) {
+  long o = 0;
+  for (long r = 0; r < (long)nstep[0] * nstep[1]; r++)
+    for (int k = 0; k < nstep[2]; k++) {
+      o_fmt_e13_5e3(v[r * nstep[2] + k], out + o);
+      o += 14;
+      /* a line with fewer than 6 numbers keeps the blank of the next
+       * (" ",...) item before the format runs out of data */
+      if (k == nstep[2] - 1 && nstep[2] % 6 != 0) out[o++] = ' ';
+      if (k % 6 == 5 || k == nstep[2] - 1) out[o++] = '\n';
+    }
+  return o;
+}
+
+/* nciplot's cutoff pass without fragments or void (nci@proc.f90:612-645) */
+long o_nci_post(const int nstep[3], const double *crho, double *cgrad, double rhocut, double dimcut,
+                double rhoplot, double srho_lo, double srho_hi, int onlyneg, double *dat) {
+  long nd = 0;
+  const long n = (long)nstep[0] * nstep[1] * nstep[2];
+  for (long v = 0; v < n; v++) {
+    if (fabs(crho[v]) < rhocut * 100.0 && cgrad[v] < dimcut) {
+      dat[2 * nd] = crho[v] / 100.0;
+      dat[2 * nd + 1] = cgrad[v];
+      nd++;
+    }
+    if (fabs(crho[v]) > rhoplot * 100.0) cgrad[v] = 100.0;
+    if (crho[v] < srho_lo * 100.0 || crho[v] > srho_hi * 100.0) cgrad[v] = 100.0;
+    if (crho[v] > 0 && onlyneg) cgrad[v] = 100.0;
+  }
+  return nd;
 }

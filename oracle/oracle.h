@@ -76,6 +76,18 @@ int o_pair_seeds(const owfn *w, double maxdist, int npts, double *xseed, int max
 int o_autocritic(const owfn *w, int nseed, const double *xseed, int nthreads, int maxcp,
                  double *cp_xyz, int *cp_typ, double *cp_f, int *nuc_count);
 
+/* NCI output (src/nci@proc.f90:612-645, 916-932).  o_fmt_e13_5e3 writes
+ * the 14 characters of (" ",1p,e13.5e3), o_fmt_E15_7 the 15 of 1p,E15.7
+ * (three-digit exponents without the E).  o_cube_body writes a cube body
+ * (records of nstep[2] numbers, 6 a line) and returns its length.
+ * o_nci_post applies the cutoff pass to cgrad in place and writes the .dat
+ * pairs into dat (room for every point); returns their number. */
+void o_fmt_e13_5e3(double x, char *out);
+void o_fmt_E15_7(double x, char *out);
+long o_cube_body(const int nstep[3], const double *v, char *out);
+long o_nci_post(const int nstep[3], const double *crho, double *cgrad, double rhocut, double dimcut,
+                double rhoplot, double srho_lo, double srho_hi, int onlyneg, double *dat);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,13 @@ def lib():
         L.o_pair_seeds.restype = C.c_int
         L.o_autocritic.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, C.c_int, _dp, _ip, _dp, _ip]
         L.o_autocritic.restype = C.c_int
+        L.o_fmt_e13_5e3.argtypes = [C.c_double, C.c_char_p]
+        L.o_fmt_E15_7.argtypes = [C.c_double, C.c_char_p]
+        L.o_cube_body.argtypes = [_ip, _dp, C.c_char_p]
+        L.o_cube_body.restype = C.c_long
+        L.o_nci_post.argtypes = [_ip, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_int, _dp]
+        L.o_nci_post.restype = C.c_long
     return _lib
 
 
@@ -191,3 +198,46 @@ def matinvsym3(m):
     a = _f64(np.asarray(m).T.reshape(-1)).copy()
     ier = lib().o_matinvsym3(a)
     return a.reshape(3, 3).T, ier
+
+
+# ------------------------------------------------------------- NCI output
+def fmt_e13(x) -> str:
+    """(" ",1p,e13.5e3) of one number (14 characters)."""
+    b = C.create_string_buffer(16)
+    lib().o_fmt_e13_5e3(float(x), b)
+    return b.raw[:14].decode()
+
+
+def fmt_E15(x) -> str:
+    """1p,E15.7 of one number (15 characters)."""
+    b = C.create_string_buffer(16)
+    lib().o_fmt_E15_7(float(x), b)
+    return b.raw[:15].decode()
+
+
+def cube_body(nstep, values) -> bytes:
+    """write_cube_body text of a (k,j,i)-ordered cube."""
+    ns = _i32(nstep)
+    v = _f64(values).reshape(-1)
+    n3 = int(ns[2])
+    size = int(ns[0]) * int(ns[1]) * (14 * n3 + (n3 + 5) // 6 + (1 if n3 % 6 else 0))
+    b = C.create_string_buffer(size + 16)
+    m = lib().o_cube_body(ns, v, b)
+    return b.raw[:m]
+
+
+def dat_text(dat) -> bytes:
+    """.dat lines (1p,E15.7,E15.7) of (n,2) pairs."""
+    d = _f64(dat).reshape(-1, 2)
+    return "".join(fmt_E15(a) + fmt_E15(b) + "\n" for a, b in d).encode()
+
+
+def nci_post(nstep, crho, cgrad, rhocut=0.2, dimcut=2.0, rhoplot=0.1, srho=(-1e30, 1e30), onlyneg=False):
+    """nciplot's cutoff pass: returns (cgrad after the s := 100 rules,
+    dat pairs (n, 2))."""
+    ns = _i32(nstep)
+    cr = _f64(crho).reshape(-1)
+    cg = _f64(cgrad).reshape(-1).copy()
+    dat = np.zeros(2 * cr.size)
+    nd = lib().o_nci_post(ns, cr, cg, rhocut, dimcut, rhoplot, srho[0], srho[1], int(onlyneg), dat)
+    return cg, dat[: 2 * nd].reshape(-1, 2)
