@@ -22,6 +22,7 @@ EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_
            "c2g_wfn_destroy", "c2g_wfn_set_param", "c2g_wfn_info", "c2g_rho2", "c2g_grd", "c2g_nciplot",
            "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
            "c2g_autocritic", "c2g_nci_post_dev", "c2g_cube_text", "c2g_dat_text", "c2g_nciplot_files",
+           "c2g_grid_field_dev", "c2g_cube_precise_text", "c2g_cube_field_file",
            # learned CP-seed proposer (include/critic2_gb300_cpseed.h)
            "c2g_cs_conv3d", "c2g_cs_conv3d_bwd_data", "c2g_cs_conv3d_bwd_weight", "c2g_cs_loss",
            "c2g_cs_targets", "c2g_cs_features", "c2g_cs_seeds", "c2g_cs_adam")
@@ -85,6 +86,9 @@ def lib():
     L.c2g_dat_text.argtypes = [_vp, C.c_long, C.c_char_p, C.c_long, C.POINTER(C.c_long), _vp]
     L.c2g_nciplot_files.argtypes = [_vp, _dp, _dp, _ip, C.c_int, C.c_char_p, C.POINTER(NciCut),
                                     C.POINTER(NciStats), _dp]
+    L.c2g_grid_field_dev.argtypes = [_vp, _dp, _dp, _ip, C.c_int, C.c_int, _vp, _vp]
+    L.c2g_cube_precise_text.argtypes = [_ip, _vp, C.c_char_p, C.c_long, C.POINTER(C.c_long), _vp]
+    L.c2g_cube_field_file.argtypes = [_vp, _dp, _dp, _ip, C.c_int, C.c_int, C.c_char_p, _dp]
     i, f, lg = C.c_int, C.c_float, C.c_long
     L.c2g_cs_conv3d.argtypes = [_vp, i, i, i, i, i, _vp, _vp, i, i, i, _vp, _vp]
     L.c2g_cs_conv3d_bwd_data.argtypes = [_vp, i, i, i, i, i, _vp, i, i, _vp, _vp, _vp]

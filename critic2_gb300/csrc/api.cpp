@@ -601,6 +601,31 @@ void write_file(const std::string &path, const std::string &head, const char *bo
   if (std::fclose(f) != 0 || !ok) fail(C2G_ERR_IO, "write failed: " + path);
 }
 
+// writegrid_cube's precise header (src/crystalmod@write.f90:3527-3545): all
+// atoms, in the frame of the handle
+void put_precise_header(std::string &o, const HostWfn &w, const double *x0, const double *xmat,
+                        const int *nstep) {
+  char f[3][24], b[160];
+  auto e22 = [&](double x, char *out) {
+    fmt_E22_14E3(x, out);
+    out[22] = 0;
+  };
+  o += "critic2-cube\ncritic2-cube\n";
+  for (int c = 0; c < 3; c++) e22(x0[c], f[c]);
+  std::snprintf(b, sizeof b, "%5d %s %s %s \n", w.natom, f[0], f[1], f[2]);
+  o += b;
+  for (int i = 0; i < 3; i++) {
+    for (int c = 0; c < 3; c++) e22(xmat[3 * i + c], f[c]);
+    std::snprintf(b, sizeof b, "%5d %s %s %s \n", nstep[i], f[0], f[1], f[2]);
+    o += b;
+  }
+  for (int a = 0; a < w.natom; a++) {
+    for (int c = 0; c < 3; c++) e22(w.xyz[3 * a + c], f[c]);
+    std::snprintf(b, sizeof b, "%5d %5.1f %s %s %s \n", w.z[a], 0.0, f[0], f[1], f[2]);
+    o += b;
+  }
+}
+
 double ms_since(std::chrono::steady_clock::time_point t) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
 }
@@ -645,6 +670,69 @@ int c2g_dat_text(const double *d_dat, long ndat, char *text, long cap, long *nby
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     DevBuf dt(nb), sc(sizeof(int) * cube_flag_scratch_ints());
     dat_text_dev(d_dat, ndat, dt.as<char>(), text, sc.as<int>(), st);
+  });
+}
+
+int c2g_grid_field_dev(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec, int prop,
+                       double *d_out, void *stream) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(x0 && xmat && nstep && d_out, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    require(prop >= 0 && prop <= 11, "unknown field property");
+    check_prec(prec);
+    DeviceGuard g(h->device);
+    GridSpec gs;
+    for (int j = 0; j < 3; j++) gs.x0[j] = x0[j], gs.nstep[j] = nstep[j];
+    for (int j = 0; j < 9; j++) gs.xmat[j] = xmat[j];
+    field_grid_dev(*h, gs, prec, prop, d_out, static_cast<cudaStream_t>(stream));
+  });
+}
+
+int c2g_cube_precise_text(const int *nstep, const double *d_values, char *text, long cap, long *nbytes,
+                          void *stream) {
+  return guarded([&] {
+    require(nstep && d_values && nbytes, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    const long nb = precise_body_bytes(nstep);
+    *nbytes = nb;
+    if (!text) return;
+    if (cap < nb) fail(C2G_ERR_ARG, "text buffer too small (" + std::to_string(nb) + " bytes needed)");
+    DevBuf dt(nb), sc(sizeof(int) * cube_flag_scratch_ints());
+    precise_text_dev(nstep, d_values, dt.as<char>(), text, sc.as<int>(), static_cast<cudaStream_t>(stream));
+  });
+}
+
+int c2g_cube_field_file(c2g_wfn *hp, const double *x0, const double *xmat, const int *nstep, int prec, int prop,
+                        const char *path, double *ms_parts) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(x0 && xmat && nstep && path, "null argument");
+    require(nstep[0] > 0 && nstep[1] > 0 && nstep[2] > 0, "nstep must be positive");
+    DeviceGuard g(h->device);
+    const long n = (long)nstep[0] * nstep[1] * nstep[2];
+    auto t0 = std::chrono::steady_clock::now();
+    DevBuf dv(sizeof(double) * n);
+    int rc = c2g_grid_field_dev(hp, x0, xmat, nstep, prec, prop, dv.as<double>(), nullptr);
+    if (rc != C2G_OK) fail(rc, g_last_error);
+    const double t_eval = ms_since(t0);
+    auto t1 = std::chrono::steady_clock::now();
+    const long nb = precise_body_bytes(nstep);
+    std::vector<char> ht(nb);
+    {
+      DevBuf dt(nb), sc(sizeof(int) * cube_flag_scratch_ints());
+      precise_text_dev(nstep, dv.as<double>(), dt.as<char>(), ht.data(), sc.as<int>(), nullptr);
+    }
+    const double t_fmt = ms_since(t1);
+    auto t2 = std::chrono::steady_clock::now();
+    std::string head;
+    put_precise_header(head, h->host, x0, xmat, nstep);
+    write_file(path, head, ht.data(), nb);
+    if (ms_parts) {
+      ms_parts[0] = t_eval;
+      ms_parts[1] = t_fmt;
+      ms_parts[2] = ms_since(t2);
+    }
   });
 }
 

@@ -25,6 +25,7 @@
 
 #include "c2g_internal.h"
 #include "k_cube.h"
+#include "k_tc.h"
 
 namespace c2g {
 
@@ -81,6 +82,34 @@ void fmt_E15_7(double x, char *out) {
 // and after the last, and one blank before that last newline when the line
 // holds fewer than 6 (Fortran writes the (" ") of the next item before it
 // finds the list exhausted).
+// Fortran E22.14E3 (no scale factor): 0.dddddddddddddd with 14 digits and
+// a 3-digit exponent, right-justified in 22 columns.
+void fmt_E22_14E3(double x, char *out) {
+  char buf[48];
+  std::snprintf(buf, sizeof buf, "%.13E", x);  // [-]d.dddddddddddddE[+-]dd[d]
+  const char *p = std::strchr(buf, 'E');
+  const int e = std::atoi(p + 1) + (x != 0.0 ? 1 : 0);
+  const bool neg = buf[0] == '-';
+  const char *m = buf + (neg ? 1 : 0);  // d.ddddddddddddd
+  char t[24];
+  t[0] = neg ? '-' : ' ';
+  t[1] = '0';
+  t[2] = '.';
+  t[3] = m[0];
+  for (int i = 0; i < 13; i++) t[4 + i] = m[2 + i];
+  t[17] = 'E';
+  t[18] = e < 0 ? '-' : '+';
+  const int ae = e < 0 ? -e : e;
+  t[19] = (char)('0' + ae / 100);
+  t[20] = (char)('0' + (ae / 10) % 10);
+  t[21] = (char)('0' + ae % 10);
+  std::memcpy(out, t, 22);
+}
+
+long precise_record_bytes(int n3) { return 23L * n3 + (n3 + 5) / 6 + (n3 % 6 ? 1 : 0); }
+
+long precise_body_bytes(const int *n) { return precise_record_bytes(n[2]) * n[0] * n[1]; }
+
 long cube_record_bytes(int n3) { return 14L * n3 + (n3 + 5) / 6 + (n3 % 6 ? 1 : 0); }
 
 long cube_body_bytes(const int *n) { return cube_record_bytes(n[2]) * n[0] * n[1]; }
@@ -198,6 +227,110 @@ __device__ bool dev_E15(double x, char *o) {
   return ok;
 }
 
+// a * 10^s as a double-double hi + lo (error ~1e-30 relative): exact
+// products with the exact powers 10^0..10^22, exact remainders for
+// divisions.
+__device__ __forceinline__ void dd_scale10(double a, int s, double &hi, double &lo) {
+  hi = a;
+  lo = 0.0;
+  while (s != 0) {
+    const int k = s > 22 ? 22 : (s < -22 ? -22 : s);
+    double p = 1.0;
+    for (int i = 0; i < (k < 0 ? -k : k); i++) p *= 10.0;
+    if (k > 0) {
+      const double h = hi * p;
+      const double e = fma(hi, p, -h);
+      hi = h;
+      lo = fma(lo, p, e);
+    } else {
+      const double q = hi / p;
+      const double r = fma(-q, p, hi);  // exact remainder
+      hi = q;
+      lo = (r + lo) / p;
+    }
+    // renormalise
+    const double t = hi + lo;
+    lo = lo - (t - hi);
+    hi = t;
+    s -= k;
+  }
+}
+
+// D significant digits (D <= 15) of a > 0 from the double-double product;
+// false when within `margin` of a rounding boundary.
+__device__ bool dd_digits(double a, int D, double margin, long long &n, int &e) {
+  double lo10 = 1.0;
+  for (int i = 1; i < D; i++) lo10 *= 10.0;
+  const double hi10 = lo10 * 10.0;
+  int e0 = (int)floor(log10(a));
+  for (int it = 0; it < 4; it++) {
+    double yh, yl;
+    dd_scale10(a, D - 1 - e0, yh, yl);
+    double r = rint(yh);
+    double f = (yh - r) + yl;  // in about [-0.5, 0.5]
+    if (f > 0.5) r += 1.0, f -= 1.0;
+    if (f <= -0.5) r -= 1.0, f += 1.0;
+    if (r >= hi10) {
+      e0++;
+      continue;
+    }
+    if (r < lo10) {
+      e0--;
+      continue;
+    }
+    n = (long long)r;
+    e = e0;
+    return fabs(fabs(f) - 0.5) > margin;
+  }
+  return false;
+}
+
+// 23 characters of " " + E22.14E3; false for a near tie
+__device__ bool dev_E22(double x, char *o) {
+  const bool neg = signbit(x);
+  const double a = fabs(x);
+  long long n = 0;
+  int e = 0;
+  bool ok = true;
+  if (a != 0.0) ok = dd_digits(a, 14, 1e-6, n, e), e += 1;
+  char t[23];
+  t[0] = ' ';
+  t[1] = neg ? '-' : ' ';
+  t[2] = '0';
+  t[3] = '.';
+  for (int i = 17; i >= 4; i--) {
+    t[i] = (char)('0' + (int)(n % 10));
+    n /= 10;
+  }
+  t[18] = 'E';
+  t[19] = e < 0 ? '-' : '+';
+  const int ae = e < 0 ? -e : e;
+  t[20] = (char)('0' + ae / 100);
+  t[21] = (char)('0' + (ae / 10) % 10);
+  t[22] = (char)('0' + ae % 10);
+  for (int i = 0; i < 23; i++) o[i] = t[i];
+  return ok;
+}
+
+__global__ void k_precise_text(const double *__restrict__ v, long n, int n3, long rec_bytes,
+                               char *__restrict__ text, int *__restrict__ flags, int *__restrict__ nflag) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long rec = i / n3;
+  const int m = (int)(i - rec * n3);
+  char *o = text + rec * rec_bytes + 23L * m + m / 6;
+  if (!dev_E22(v[i], o)) {
+    const int s = atomicAdd(nflag, 1);
+    if (s < kFlagCap) flags[s] = (int)i;
+  }
+  if (m == n3 - 1 && n3 % 6 != 0) {
+    o[23] = ' ';
+    o[24] = '\n';
+  } else if (m % 6 == 5) {
+    o[23] = '\n';
+  }
+}
+
 __global__ void k_cube_text(const double *__restrict__ v, long n, int n3, long rec_bytes, char *__restrict__ text,
                             int *__restrict__ flags, int *__restrict__ nflag) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -311,7 +444,8 @@ __global__ void k_post_apply(const double *__restrict__ crho, double *__restrict
   }
 }
 
-void fix_flags(const int *d_flags, const int *d_nflag, const double *d_v, char *text, bool on_device, bool cube,
+// mode: 0 cube e13.5e3, 1 dat E15.7, 2 cube E22.14E3
+void fix_flags(const int *d_flags, const int *d_nflag, const double *d_v, char *text, bool on_device, int mode,
                int n3, long rec_bytes, cudaStream_t st) {
   int nf = 0;
   C2G_CUDA(cudaMemcpyAsync(&nf, d_nflag, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -324,15 +458,21 @@ void fix_flags(const int *d_flags, const int *d_nflag, const double *d_v, char *
     const long i = idx[q];
     double x = 0.0;
     C2G_CUDA(cudaMemcpy(&x, d_v + i, sizeof(double), cudaMemcpyDeviceToHost));
-    char buf[16];
+    char buf[32];
     long off;
     int len;
-    if (cube) {
+    if (mode == 0) {
       const long rec = i / n3;
       const int m = (int)(i - rec * n3);
       off = rec * rec_bytes + 14L * m + m / 6;
       fmt_e13_5e3(x, buf);
       len = 14;
+    } else if (mode == 2) {
+      const long rec = i / n3;
+      const int m = (int)(i - rec * n3);
+      off = rec * rec_bytes + 23L * m + m / 6 + 1;  // after the separator blank
+      fmt_E22_14E3(x, buf);
+      len = 22;
     } else {
       off = (i >> 1) * 31 + 15 * (i & 1);
       fmt_E15_7(x, buf);
@@ -357,9 +497,27 @@ void cube_text_dev(const int *nstep, const double *d_v, char *d_text, char *h_te
   }
   if (h_text) {
     C2G_CUDA(cudaMemcpyAsync(h_text, d_text, (size_t)(rb * nstep[0] * nstep[1]), cudaMemcpyDeviceToHost, st));
-    fix_flags(flags, nflag, d_v, h_text, false, true, nstep[2], rb, st);
+    fix_flags(flags, nflag, d_v, h_text, false, 0, nstep[2], rb, st);
   } else {
-    fix_flags(flags, nflag, d_v, d_text, true, true, nstep[2], rb, st);
+    fix_flags(flags, nflag, d_v, d_text, true, 0, nstep[2], rb, st);
+  }
+}
+
+void precise_text_dev(const int *nstep, const double *d_v, char *d_text, char *h_text, int *d_scratch,
+                      cudaStream_t st) {
+  const long n = (long)nstep[0] * nstep[1] * nstep[2];
+  const long rb = precise_record_bytes(nstep[2]);
+  int *nflag = d_scratch, *flags = d_scratch + 8;
+  C2G_CUDA(cudaMemsetAsync(nflag, 0, sizeof(int), st));
+  if (n > 0) {
+    k_precise_text<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_v, n, nstep[2], rb, d_text, flags, nflag);
+    C2G_CUDA(cudaGetLastError());
+  }
+  if (h_text) {
+    C2G_CUDA(cudaMemcpyAsync(h_text, d_text, (size_t)(rb * nstep[0] * nstep[1]), cudaMemcpyDeviceToHost, st));
+    fix_flags(flags, nflag, d_v, h_text, false, 2, nstep[2], rb, st);
+  } else {
+    fix_flags(flags, nflag, d_v, d_text, true, 2, nstep[2], rb, st);
   }
 }
 
@@ -372,9 +530,9 @@ void dat_text_dev(const double *d_dat, long ndat, char *d_text, char *h_text, in
   }
   if (h_text) {
     C2G_CUDA(cudaMemcpyAsync(h_text, d_text, (size_t)(31 * ndat), cudaMemcpyDeviceToHost, st));
-    fix_flags(flags, nflag, d_dat, h_text, false, false, 0, 0, st);
+    fix_flags(flags, nflag, d_dat, h_text, false, 1, 0, 0, st);
   } else {
-    fix_flags(flags, nflag, d_dat, d_text, true, false, 0, 0, st);
+    fix_flags(flags, nflag, d_dat, d_text, true, 1, 0, 0, st);
   }
 }
 
@@ -396,5 +554,86 @@ long nci_post_dev(const int *nstep, const double *d_crho, double *d_cgrad, const
 }
 
 int cube_flag_scratch_ints() { return 8 + kFlagCap; }
+
+namespace {
+
+// grid points x0 + i xmat(:,1) + j xmat(:,2) + k xmat(:,3), k fastest, for
+// the i-planes [i0, i0 + ni)
+__global__ void k_grid_points(GridSpec g, int i0, long n, double *__restrict__ xyz) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long plane = (long)g.nstep[1] * g.nstep[2];
+  const int i = i0 + (int)(t / plane);
+  const long r = t % plane;
+  const int j = (int)(r / g.nstep[2]), k = (int)(r % g.nstep[2]);
+  for (int c = 0; c < 3; c++) xyz[3 * t + c] = g.x0[c] + i * g.xmat[c] + j * g.xmat[3 + c] + k * g.xmat[6 + c];
+}
+
+// one grd quantity per point from a (rho, grad, hess) record; the gradient
+// is zero within 1e-5 bohr of a nucleus (src/fieldmod@proc.f90:1148-1154)
+__global__ void k_field_prop(const double *__restrict__ rec, const double *__restrict__ xyz, long n, int prop,
+                             const double4 *__restrict__ atoms, int natom, double *__restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double *r = rec + 10 * t;
+  double g[3] = {r[1], r[2], r[3]};
+  if (prop >= 1 && prop <= 4) {
+    for (int a = 0; a < natom; a++) {
+      const double4 A = atoms[a];
+      const double dx = xyz[3 * t] - A.x, dy = xyz[3 * t + 1] - A.y, dz = xyz[3 * t + 2] - A.z;
+      if (dx * dx + dy * dy + dz * dz <= 1e-10) g[0] = g[1] = g[2] = 0.0;
+    }
+  }
+  double v;
+  switch (prop) {
+    case 0: v = r[0]; break;
+    case 1: v = g[0]; break;
+    case 2: v = g[1]; break;
+    case 3: v = g[2]; break;
+    case 4: v = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]); break;
+    case 5: v = r[4]; break;  // hxx
+    case 6: v = r[7]; break;  // hxy
+    case 7: v = r[8]; break;  // hxz
+    case 8: v = r[5]; break;  // hyy
+    case 9: v = r[9]; break;  // hyz
+    case 10: v = r[6]; break;  // hzz
+    default: v = r[4] + r[5] + r[6]; break;  // laplacian
+  }
+  out[t] = v;
+}
+
+}  // namespace
+
+void field_grid_dev(Handle &h, const GridSpec &g, int prec, int prop, double *d_out, cudaStream_t st) {
+  const long plane = (long)g.nstep[1] * g.nstep[2];
+  const int nip = (int)std::max(1L, std::min((long)g.nstep[0], (4L << 20) / std::max(1L, plane)));
+  const long cap = (long)nip * plane;
+  double *xyz = nullptr, *rec = nullptr;
+  if (cudaMalloc(&xyz, sizeof(double) * 3 * cap) != cudaSuccess) fail(C2G_ERR_ALLOC, "cudaMalloc (grid points)");
+  if (cudaMalloc(&rec, sizeof(double) * 10 * cap) != cudaSuccess) {
+    cudaFree(xyz);
+    fail(C2G_ERR_ALLOC, "cudaMalloc (grid records)");
+  }
+  try {
+    for (int i0 = 0; i0 < g.nstep[0]; i0 += nip) {
+      const int ni = std::min(nip, g.nstep[0] - i0);
+      const long n = (long)ni * plane;
+      k_grid_points<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, i0, n, xyz);
+      C2G_CUDA(cudaGetLastError());
+      if (prec == C2G_PREC_FP64) launch_fp64_points(h.dev, (int)n, xyz, 2, false, rec, st);
+      else tc_points(h, prec, (int)n, xyz, rec, st);
+      k_field_prop<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rec, xyz, n, prop, h.dev.atoms, h.dev.natom,
+                                                                d_out + (long)i0 * plane);
+      C2G_CUDA(cudaGetLastError());
+    }
+    C2G_CUDA(cudaStreamSynchronize(st));
+  } catch (...) {
+    cudaFree(xyz);
+    cudaFree(rec);
+    throw;
+  }
+  cudaFree(xyz);
+  cudaFree(rec);
+}
 
 }  // namespace c2g

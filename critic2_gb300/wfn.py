@@ -158,6 +158,18 @@ class Wavefunction:
                                           C.byref(c) if c is not None else None, C.byref(st), ms))
         return st, ms
 
+    FIELDS = ("rho", "gx", "gy", "gz", "gmod", "hxx", "hxy", "hxz", "hyy", "hyz", "hzz", "lap")
+
+    def cube_field_file(self, x0, xmat, nstep, prop, path: str, prec="fp64"):
+        """CUBE plot of one grd quantity (name in FIELDS) into a precise
+        critic2 cube file (c2g_cube_field_file); returns the wall times in
+        ms of evaluation, text and write."""
+        ms = np.zeros(3)
+        xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+        L.check(L.lib().c2g_cube_field_file(self._h, _f64(x0), xm, _i32(nstep), _prec(prec),
+                                            self.FIELDS.index(prop), path.encode(), ms))
+        return ms
+
     # -------------------------------------------------------------- Newton
     def newton(self, xyz, gfnormeps: float = 1e-12, maxit: int = 200, prec="fp64"):
         x = _f64(xyz).reshape(-1, 3).copy()

@@ -217,6 +217,39 @@ int c2g_dat_text(const double *d_dat, long ndat, char *text, long cap, long *nby
 int c2g_nciplot_files(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec,
                       const char *root, const c2g_nci_cut *cut, c2g_nci_stats *stats, double *ms_parts);
 
+/* Quantities of field%grd for CUBE plots (rhoplot_cube's nti selectors,
+ * src/rhoplot@proc.f90:905-930). */
+#define C2G_FIELD_RHO 0
+#define C2G_FIELD_GX 1
+#define C2G_FIELD_GY 2
+#define C2G_FIELD_GZ 3
+#define C2G_FIELD_GMOD 4
+#define C2G_FIELD_HXX 5
+#define C2G_FIELD_HXY 6
+#define C2G_FIELD_HXZ 7
+#define C2G_FIELD_HYY 8
+#define C2G_FIELD_HYZ 9
+#define C2G_FIELD_HZZ 10
+#define C2G_FIELD_LAP 11
+
+/* rhoplot_cube's evaluation (src/rhoplot@proc.f90:890-950): one
+ * C2G_FIELD_* quantity of grd at x0 + i*xmat(:,1) + j*xmat(:,2) +
+ * k*xmat(:,3) into the device array d_out, (k,j,i) order (k fastest). */
+int c2g_grid_field_dev(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec, int prop,
+                       double *d_out, void *stream);
+
+/* writegrid_cube's precise body (src/crystalmod@write.f90:3557-3567,
+ * (6(" ",E22.14E3)) records) of a device cube into the host buffer text,
+ * as c2g_cube_text. */
+int c2g_cube_precise_text(const int *nstep, const double *d_values, char *text, long cap, long *nbytes,
+                          void *stream);
+
+/* CUBE plot end to end: c2g_grid_field_dev + a precise cube file (header as
+ * writegrid_cube, all atoms, in the frame of the handle).  ms_parts (may be
+ * NULL) receives 3 wall times in ms: evaluation, text, file write. */
+int c2g_cube_field_file(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec, int prop,
+                        const char *path, double *ms_parts);
+
 /* field%newton for n seeds at once (src/fieldmod@proc.f90:2238-2279):
  * xyz(3,n) in/out; ier(n): 0 converged (|grad| < gfnormeps), 1 invalid or
  * singular Hessian, 2 maxit reached.  In the split modes the iterations run

@@ -786,3 +786,22 @@ long o_nci_post(const int nstep[3], const double *crho, double *cgrad, double rh
   }
   return nd;
 }
+
+/* E22.14E3 without scale factor (writegrid_cube's precise format,
+ * src/crystalmod@write.f90:3536-3563): 0.dddddddddddddd (14 digits) and
+ * a 3-digit exponent, right-justified in 22 columns. */
+void o_fmt_E22_14E3(double x, char *out) {
+  char buf[64], t[96];
+  snprintf(buf, sizeof buf, "%.13E", x);
+  char *p = strchr(buf, 'E');
+  int e = atoi(p + 1) + (x != 0.0 ? 1 : 0);
+  *p = 0;
+  const int neg = buf[0] == '-';
+  const char *m = buf + neg; /* d.ddddddddddddd */
+  char dig[16];
+  dig[0] = m[0];
+  memcpy(dig + 1, m + 2, 13);
+  dig[14] = 0;
+  snprintf(t, sizeof t, "%c0.%sE%c%03d", neg ? '-' : ' ', dig, e < 0 ? '-' : '+', e < 0 ? -e : e);
+  memcpy(out, t, 22);
+}

@@ -84,6 +84,7 @@ int o_autocritic(const owfn *w, int nseed, const double *xseed, int nthreads, in
  * pairs into dat (room for every point); returns their number. */
 void o_fmt_e13_5e3(double x, char *out);
 void o_fmt_E15_7(double x, char *out);
+void o_fmt_E22_14E3(double x, char *out);
 long o_cube_body(const int nstep[3], const double *v, char *out);
 long o_nci_post(const int nstep[3], const double *crho, double *cgrad, double rhocut, double dimcut,
                 double rhoplot, double srho_lo, double srho_hi, int onlyneg, double *dat);

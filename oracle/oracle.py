@@ -73,6 +73,7 @@ def lib():
         L.o_autocritic.restype = C.c_int
         L.o_fmt_e13_5e3.argtypes = [C.c_double, C.c_char_p]
         L.o_fmt_E15_7.argtypes = [C.c_double, C.c_char_p]
+        L.o_fmt_E22_14E3.argtypes = [C.c_double, C.c_char_p]
         L.o_cube_body.argtypes = [_ip, _dp, C.c_char_p]
         L.o_cube_body.restype = C.c_long
         L.o_nci_post.argtypes = [_ip, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -241,3 +242,23 @@ def nci_post(nstep, crho, cgrad, rhocut=0.2, dimcut=2.0, rhoplot=0.1, srho=(-1e3
     dat = np.zeros(2 * cr.size)
     nd = lib().o_nci_post(ns, cr, cg, rhocut, dimcut, rhoplot, srho[0], srho[1], int(onlyneg), dat)
     return cg, dat[: 2 * nd].reshape(-1, 2)
+
+
+def fmt_E22(x) -> str:
+    """E22.14E3 (no scale factor) of one number (22 characters)."""
+    b = C.create_string_buffer(24)
+    lib().o_fmt_E22_14E3(float(x), b)
+    return b.raw[:22].decode()
+
+
+def precise_body(nstep, values) -> str:
+    """writegrid_cube's (6(" ",E22.14E3)) body of a (k,j,i)-ordered cube."""
+    ns = [int(v) for v in nstep]
+    v = _f64(values).reshape(-1)
+    out = []
+    for r in range(ns[0] * ns[1]):
+        row = v[r * ns[2]:(r + 1) * ns[2]]
+        for c in range(0, ns[2], 6):
+            chunk = row[c:c + 6]
+            out.append("".join(" " + fmt_E22(x) for x in chunk) + (" " if len(chunk) < 6 else "") + "\n")
+    return "".join(out)

@@ -48,6 +48,17 @@ def main():
         "dat_lines_total": len([l for l in dat if l]),
         "dat_lines": [l for l in dat if l][::29],
     }
+    # writegrid_cube's precise cubes (tests/005_plot/ref): header lines and
+    # a sample of body lines
+    pre = {}
+    for name in ("013_cube_simple_07.cube", "016_cube_grid_01.cube"):
+        with open(os.path.join(REF, "tests", "005_plot", "ref", name)) as f:
+            lines = f.read().split("\n")
+        nat = int(lines[2].split()[0])
+        body = [l for l in lines[6 + nat:] if l]
+        pre[name] = {"header": lines[:6 + nat], "nstep": [int(lines[3 + c].split()[0]) for c in range(3)],
+                     "body_lines": len(body), "sample": body[::13]}
+    out["precise_cubes"] = pre
     with open(os.path.join(HERE, "nci_cube_text.json"), "w") as f:
         json.dump(out, f, indent=0)
     print("wrote", len(out["dens_lines"]), "body lines per cube and", len(out["dat_lines"]), "dat lines")

@@ -126,3 +126,65 @@ def test_nciplot_files(gpu_lib, oracle_mod):
     assert grad[head_len + (len(hg[0]) - len(hd[0])) + (len(hg[1]) - len(hd[1])):] == \
         oracle_mod.cube_body(ns, cg_ref)
     assert dat == oracle_mod.dat_text(dat_ref)
+
+
+def precise_text(L, lib, ns, vals):
+    d = torch.tensor(np.ascontiguousarray(vals, np.float64).reshape(-1), device="cuda")
+    n = C.c_long(0)
+    ns = np.ascontiguousarray(ns, np.int32)
+    lib.check(L.c2g_cube_precise_text(ns, _p(d), None, 0, C.byref(n), None))
+    buf = C.create_string_buffer(n.value + 1)
+    lib.check(L.c2g_cube_precise_text(ns, _p(d), buf, n.value + 1, C.byref(n), None))
+    return buf.raw[: n.value].decode()
+
+
+@pytest.mark.parametrize("ns", [(3, 4, 10), (2, 2, 12)])
+def test_precise_text_matches_oracle(gpu_lib, oracle_mod, ns):
+    L = gpu_lib.lib()
+    rng = np.random.default_rng(sum(ns) + 1)
+    v = wide_values(rng, int(np.prod(ns)))
+    assert precise_text(L, gpu_lib, ns, v) == oracle_mod.precise_body(ns, v)
+
+
+def test_precise_text_reproduces_reference(gpu_lib):
+    L = gpu_lib.lib()
+    with open(os.path.join(HERE, "golden", "nci_cube_text.json")) as f:
+        gold = json.load(f)
+    for c in gold["precise_cubes"].values():
+        for k in (6, 4):
+            sel = [l for l in c["sample"] if len(l.split()) == k]
+            if not sel:
+                continue
+            vals = np.array([[float(t) for t in l.split()] for l in sel])
+            assert precise_text(L, gpu_lib, (len(sel), 1, k), vals) == "".join(l + "\n" for l in sel)
+
+
+def test_cube_field_file(gpu_lib, oracle_mod):
+    """CUBE plots of rho, |grad rho| and the Laplacian on the 12-atom molecule:
+    values against the oracle's grd (1e-10), text against the oracle's
+    formatting of the same values, header as writegrid_cube."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("nci12")
+    w = Wavefunction(mol)
+    o = oracle_mod.Wfn(mol)
+    x0, xm, _ = synth.nci_grid(mol, 24, 0.25)
+    ns = np.array([24, 20, 17], np.int32)
+    pts = synth.grid_points(x0, xm, ns).reshape(-1, 3)
+    idx = np.random.default_rng(1).choice(len(pts), 60, replace=False)
+    with tempfile.TemporaryDirectory() as d:
+        for prop in ("rho", "gmod", "lap", "hxy"):
+            path = os.path.join(d, prop + ".cube")
+            w.cube_field_file(x0, xm, ns, prop, path, "fp64")
+            txt = open(path).read()
+            lines = txt.split("\n")
+            assert lines[0] == "critic2-cube" and lines[1] == "critic2-cube"
+            assert int(lines[2].split()[0]) == mol.natom
+            body = "\n".join(lines[6 + mol.natom:])
+            vals = np.array([float(t) for t in body.split()])
+            assert vals.size == pts.shape[0]
+            assert body == oracle_mod.precise_body(ns, vals)
+            for i in idx:
+                r = o.grd(pts[i], 2)
+                h = np.array(r.hf[:]).reshape(3, 3)
+                ref = {"rho": r.f, "gmod": r.gfmod, "lap": np.trace(h), "hxy": h[0, 1]}[prop]
+                assert abs(vals[i] - ref) <= 1e-10 * max(abs(ref), 1e-6 * abs(r.f)), (prop, vals[i], ref)

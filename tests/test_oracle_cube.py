@@ -88,3 +88,22 @@ def test_nci_post_restatement(oracle_mod):
     assert np.array_equal(cg, np.where(np.abs(crho) > 10, 100.0, cgrad))
     cg2, _ = oracle_mod.nci_post(ns, crho, cgrad, onlyneg=True, srho=(-0.05, 1.0))
     assert np.all(cg2[(crho > 0) | (crho < -5)] == 100.0)
+
+
+def test_precise_cube_format(oracle_mod, gold):
+    """writegrid_cube's E22.14E3 text: the sampled body lines and the header
+    numbers of the reference's tests/005_plot cubes are reproduced exactly."""
+    for name, c in gold["precise_cubes"].items():
+        n3 = c["nstep"][2]
+        assert c["body_lines"] == c["nstep"][0] * c["nstep"][1] * ((n3 + 5) // 6)
+        for line in c["sample"]:
+            vals = [float(t) for t in line.split()]
+            want = "".join(" " + oracle_mod.fmt_E22(v) for v in vals) + (" " if len(vals) < 6 else "")
+            assert want == line, name
+        for line in c["header"][2:]:
+            toks = line.split()
+            nums = [float(t) for t in toks if "E" in t]
+            for v in nums:
+                assert oracle_mod.fmt_E22(v) in line
+    assert oracle_mod.fmt_E22(0.0) == " 0.00000000000000E+000"
+    assert oracle_mod.fmt_E22(-1.0) == "-0.10000000000000E+001"
