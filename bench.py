@@ -13,7 +13,8 @@ reported beside it.  `cp_search` holds the metric's second part: the wall
 time of AUTO's critical-point search on the 100-atom molecule with critic2's
 pair seeds and with the learned seeds (recall of the plain CP list,
 Poincare-Hopf sums, seeds used), in FP64 and in TF32x3 with FP64 final
-Newton steps.
+Newton steps, with critic2's Newton and with the optional stall exit
+(C2G_PARAM_NEWTON_STALL = 30).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--prec MODE]
                   [--workload NAME] [--impl ours|reference]
@@ -162,6 +163,18 @@ def run_reference(args, wl, mol):
                                                 "nciplot loop (reference Fortran unbuildable here)"},
             "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    if not args.no_cp:
+        # the metric's second part on the CPU: AUTO with critic2's pair seeds
+        # on the 100-atom molecule, all host threads
+        from oracle import oracle
+        cmol = synth.make_molecule("cp100")
+        o = oracle.Wfn(cmol)
+        t0 = time.perf_counter()
+        r = o.autocritic(nthreads=threads)
+        line["cp_search"] = {"workload": f"cp100: {cmol.natom} atoms, {cmol.npri} primitives, {cmol.nmo} MOs",
+                             "unit": "ms", "ms_plain": 1e3 * (time.perf_counter() - t0),
+                             "ncp": int(len(r["xyz"])), "ph": int(r["ph"]), "cores": threads,
+                             "kind": "port"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -178,9 +191,10 @@ def cp_search(args):
     out = {"workload": f"cp100: {mol.natom} atoms, {mol.npri} primitives, {mol.nmo} MOs; "
                        f"proposer on a {cpseed.S_DEFAULT}^3 grid at {cpseed.H_DEFAULT} bohr",
            "unit": "ms", "higher_is_better": False}
-    for prec in args.cp_prec.split(","):
-        st = cpseed.evaluate(mol, net, prec)
-        out[prec] = {k: st[k] for k in ("ms_plain", "ms_learned", "speedup", "recall", "recall_outside_cores",
+    for mode in args.cp_modes.split(","):
+        prec, stall = mode.split(":")
+        st = cpseed.evaluate(mol, net, prec, int(stall))
+        out[f"{prec}, newton_stall {stall}"] = {k: st[k] for k in ("ms_plain", "ms_learned", "speedup", "recall", "recall_outside_cores",
                                         "ncp", "ncp_outside_cores", "plain_ph", "learned_ph", "stage", "reason",
                                         "plain_seeds", "learned_seeds", "proposal", "grid_seeds")}
     return out
@@ -201,7 +215,8 @@ def main():
     ap.add_argument("--no-cp", action="store_true", help="skip the CP-search part")
     ap.add_argument("--no-files", action="store_true", help="skip the cube/dat output part")
     ap.add_argument("--fp64-planes", type=int, default=0, help="FP64 comparison on this many i-planes")
-    ap.add_argument("--cp-prec", default="fp64,tf32x3")
+    ap.add_argument("--cp-modes", default="fp64:0,fp64:30,tf32x3:30",
+                    help="CP-search precision:stall pairs (stall 0 = critic2's Newton)")
     args = ap.parse_args()
     wl = synth.WORKLOADS[args.workload]
     if args.grid > 0:

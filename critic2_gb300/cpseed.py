@@ -467,13 +467,15 @@ def train(samples: List[Sample], epochs: int, batch: int, lr: float, S: int, see
     return net
 
 
-def evaluate(mol, net: SeedNet, prec: str = "fp64") -> dict:
+def evaluate(mol, net: SeedNet, prec: str = "fp64", stall: int = 0) -> dict:
     """Plain AUTO (critic2's pair seeds) against the learned search on one
     molecule, with the non-learned coarse-grid seeds (minima of s) as the
-    method without the network.  Times are wall times of whole searches."""
+    method without the network.  Times are wall times of whole searches.
+    stall: C2G_PARAM_NEWTON_STALL for every search (0 = critic2's Newton)."""
     from .wfn import Wavefunction
     torch = _torch()
     w = Wavefunction(mol)
+    w.set_newton_stall(stall)
 
     def timed(f, *a):
         torch.cuda.synchronize()
@@ -488,7 +490,7 @@ def evaluate(mol, net: SeedNet, prec: str = "fp64") -> dict:
         got = learned_autocritic(w, net, prec)
         grid, ms_grid = timed(lambda: w.autocritic(grid_seeds(w), prec))
         prop = got["proposal"]
-        out = dict(molecule=mol.name, natom=mol.natom, prec=prec, plain_ph=int(ref["ph"]),
+        out = dict(molecule=mol.name, natom=mol.natom, prec=prec, newton_stall=stall, plain_ph=int(ref["ph"]),
                    plain_seeds=int(ref["nseed"]), ms_plain=round(ms_plain, 1),
                    learned_ph=int(got["ph"]), stage=got["stage"], reason=got["reason"],
                    learned_seeds=int(got["seeds_used"]), ms_learned=round(got["ms"], 1),

@@ -366,6 +366,9 @@ int c2g_wfn_set_param(c2g_wfn *hp, int param, double value) {
     if (param == C2G_PARAM_RECHECK_REL) {
       require(value < 1.0, "re-check threshold must be below 1 (negative: the default)");
       tc_set_recheck(*h, value < 0.0 ? -1.0 : value);
+    } else if (param == C2G_PARAM_NEWTON_STALL) {
+      require(value >= 0.0 && value <= 1e6, "stall count must be in [0, 1e6]");
+      h->newton_stall = (int)value;
     } else {
       fail(C2G_ERR_ARG, "unknown parameter");
     }

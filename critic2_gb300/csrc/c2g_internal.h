@@ -103,6 +103,7 @@ struct Handle {
   DevWfn dev{};
   std::vector<void *> allocations;
   TcOperands *tc = nullptr;
+  int newton_stall = 0;  // C2G_PARAM_NEWTON_STALL (0: critic2's maxit only)
 };
 
 // per-point record produced by the evaluator (FP64 path), quantities:

@@ -30,6 +30,9 @@ struct NewtonCtx {
   int natom;
   double cell_lo[3], cell_aa[3];
   double gfnormeps;
+  int stall;        // > 0: stop after this many FP64 steps without a new minimum of |grad|
+  double *gbest;    // per seed: smallest FP64 |grad| so far
+  int *nstall;      // per seed: FP64 steps since that minimum
 };
 
 // mode: 0 = FP64 list, 1 = split list.  Split seeds whose step falls below
@@ -61,6 +64,17 @@ __global__ void k_newton_step(NewtonCtx c, const double *rec, double *x, const i
   double g0 = r[1], g1 = r[2], g2 = r[3];
   if (nuc) g0 = g1 = g2 = 0.0;
   const double gmod = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+  if (mode == 0 && c.stall > 0 && !(gmod < c.gfnormeps)) {
+    // |grad| stuck at the FP64 rounding floor above gfnormeps: the seed
+    // would only end at maxit (ier = 2)
+    if (gmod < c.gbest[i]) {
+      c.gbest[i] = gmod;
+      c.nstall[i] = 0;
+    } else if (++c.nstall[i] >= c.stall) {
+      ier[i] = 2;
+      return;
+    }
+  }
   if (gmod < c.gfnormeps) {
     if (mode == 0) {
       ier[i] = 0;
@@ -91,11 +105,13 @@ __global__ void k_newton_step(NewtonCtx c, const double *rec, double *x, const i
   else nextsp[atomicAdd(countsp, 1)] = i;
 }
 
-__global__ void k_iota(int *v, int n, int *count, int *ier) {
+__global__ void k_iota(int *v, int n, int *count, int *ier, double *gbest, int *nstall) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     v[i] = i;
     ier[i] = 2;
+    gbest[i] = 1e300;
+    nstall[i] = 0;
   }
   if (i == 0) *count = n;
 }
@@ -108,21 +124,24 @@ void newton_batch_dev(Handle &h, int n, double *d_x, int *d_ier, double gfnormep
   if (n <= 0) return;
   const DevWfn &w = h.dev;
   NewtonCtx c{w.atoms, w.natom, {w.cell_lo[0], w.cell_lo[1], w.cell_lo[2]},
-              {w.cell_aa[0], w.cell_aa[1], w.cell_aa[2]}, gfnormeps};
+              {w.cell_aa[0], w.cell_aa[1], w.cell_aa[2]}, gfnormeps, h.newton_stall, nullptr, nullptr};
   int *buf = nullptr;
   double *rec = nullptr;
-  C2G_CUDA(cudaMalloc(&buf, sizeof(int) * (4 * (size_t)n + 8)));
-  cudaError_t er = cudaMalloc(&rec, sizeof(double) * kRecNci * (size_t)n);
+  C2G_CUDA(cudaMalloc(&buf, sizeof(int) * (5 * (size_t)n + 8)));
+  cudaError_t er = cudaMalloc(&rec, sizeof(double) * (kRecNci + 1) * (size_t)n);
   if (er != cudaSuccess) {
     cudaFree(buf);
     fail(C2G_ERR_ALLOC, "cudaMalloc (newton records)");
   }
   int *l64[2] = {buf, buf + n}, *lsp[2] = {buf + 2 * n, buf + 3 * n};
   int *cnt = buf + 4 * n;  // cnt[0..1] fp64 counts, cnt[2..3] split counts
+  c.nstall = buf + 4 * n + 8;
+  c.gbest = rec + (size_t)kRecNci * n;
   try {
     const bool split = (prec != C2G_PREC_FP64);
     C2G_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * 8, st));
-    k_iota<<<(n + 255) / 256, 256, 0, st>>>(split ? lsp[0] : l64[0], n, split ? cnt + 2 : cnt, d_ier);
+    k_iota<<<(n + 255) / 256, 256, 0, st>>>(split ? lsp[0] : l64[0], n, split ? cnt + 2 : cnt, d_ier, c.gbest,
+                                            c.nstall);
     C2G_CUDA(cudaGetLastError());
     int cur = 0;
     int h64 = split ? 0 : n, hsp = split ? n : 0;

@@ -79,6 +79,11 @@ class Wavefunction:
         mode's default (TF32x3 1e-4, BF16x3 1e-3), 0 disables it."""
         L.check(L.lib().c2g_wfn_set_param(self._h, 1, float(rel)))
 
+    def set_newton_stall(self, k: int):
+        """Stop a Newton seed after k FP64 steps without a new minimum of
+        |grad| (C2G_PARAM_NEWTON_STALL; 0 = off, critic2's semantics)."""
+        L.check(L.lib().c2g_wfn_set_param(self._h, 2, float(k)))
+
     # ------------------------------------------------------------ rho2/grd
     def rho2(self, xyz, nder: int = 2, prec="fp64") -> dict:
         """molwfn%rho2 at points xyz (n,3).  Arrays are per point:

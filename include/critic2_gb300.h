@@ -97,6 +97,15 @@ int c2g_wfn_destroy(c2g_wfn *h);
                                    negative value): 1e-4 for TF32X3, 1e-3
                                    for BF16X3; 0 disables the re-check;
                                    values above 1e-3 act as 1e-3 */
+#define C2G_PARAM_NEWTON_STALL 2 /* Newton (c2g_newton, c2g_autocritic): stop a
+                                    seed with ier = 2 after this many FP64
+                                    steps without a new minimum of |grad|.
+                                    Default 0: off, critic2's semantics (only
+                                    maxit ends a seed).  Such seeds sit at the
+                                    FP64 rounding floor of |grad| above
+                                    gfnormeps and would otherwise run to maxit;
+                                    this option has no counterpart in the
+                                    reference. */
 int c2g_wfn_set_param(c2g_wfn *h, int param, double value);
 
 /* Sizes after pruning. */

@@ -218,3 +218,23 @@ def test_error_paths(pair12, gpu_lib):
     assert e.value.code == 1
     with pytest.raises(gpu_lib.C2GError):
         g.nciplot(np.zeros(3), np.eye(3), [0, 4, 4])
+
+
+def test_newton_stall_option(pair12):
+    """C2G_PARAM_NEWTON_STALL (off by default): seeds that converge without
+    it converge to the same points with it, and a seed it stops sits at the
+    FP64 rounding floor of |grad|."""
+    g, o = pair12
+    seeds = g.pair_seeds()[::5]
+    x0, ier0 = g.newton(seeds, 1e-12, 200, "fp64")
+    g.set_newton_stall(30)
+    try:
+        x1, ier1 = g.newton(seeds, 1e-12, 200, "fp64")
+    finally:
+        g.set_newton_stall(0)
+    both = (ier0 == 0) & (ier1 == 0)
+    assert np.array_equal(x0[both], x1[both])
+    lost = (ier0 == 0) & (ier1 != 0)
+    assert lost.sum() <= max(2, 0.02 * (ier0 == 0).sum())
+    for i in np.nonzero(lost)[0]:
+        assert noise_floor(o, x1[i])
