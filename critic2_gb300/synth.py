@@ -38,16 +38,23 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-# critic2 li(3,56) table restricted to s..f (rows 1-20), 1-based type index.
+# critic2's li(3,56) table (src/wfn_private@proc.F90:3186-3196): Cartesian
+# exponents of types 1-56 (s; p; d; f; g 21-35; h 36-56), 1-based type index.
 LI = np.array([
     (0, 0, 0),
     (1, 0, 0), (0, 1, 0), (0, 0, 1),
     (2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1),
     (3, 0, 0), (0, 3, 0), (0, 0, 3), (2, 1, 0), (2, 0, 1), (0, 2, 1),
     (1, 2, 0), (1, 0, 2), (0, 1, 2), (1, 1, 1),
+    (4, 0, 0), (0, 4, 0), (0, 0, 4), (3, 1, 0), (3, 0, 1), (1, 3, 0), (0, 3, 1), (1, 0, 3),
+    (0, 1, 3), (2, 2, 0), (2, 0, 2), (0, 2, 2), (2, 1, 1), (1, 2, 1), (1, 1, 2),
+    (0, 0, 5), (0, 1, 4), (0, 2, 3), (0, 3, 2), (0, 4, 1), (0, 5, 0), (1, 0, 4), (1, 1, 3),
+    (1, 2, 2), (1, 3, 1), (1, 4, 0), (2, 0, 3), (2, 1, 2), (2, 2, 1), (2, 3, 0), (3, 0, 2),
+    (3, 1, 1), (3, 2, 0), (4, 0, 1), (4, 1, 0), (5, 0, 0),
 ], dtype=np.int32)
 
-SHELL_TYPES = {"s": [1], "p": [2, 3, 4], "d": list(range(5, 11)), "f": list(range(11, 21))}
+SHELL_TYPES = {"s": [1], "p": [2, 3, 4], "d": list(range(5, 11)), "f": list(range(11, 21)),
+               "g": list(range(21, 36)), "h": list(range(36, 57))}
 HEAVY_Z = (6, 7, 8)
 
 

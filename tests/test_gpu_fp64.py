@@ -238,3 +238,37 @@ def test_newton_stall_option(pair12):
     assert lost.sum() <= max(2, 0.02 * (ier0 == 0).sum())
     for i in np.nonzero(lost)[0]:
         assert noise_floor(o, x1[i])
+
+
+def gh_molecule():
+    """nci12 plus one g and one h shell on every heavy atom (li types 21-56)."""
+    mol = synth.make_molecule("nci12")
+    rng = np.random.default_rng(21)
+    ic, it, e = list(mol.icenter), list(mol.itype), list(mol.e)
+    for a in np.nonzero(mol.atom_z != 1)[0]:
+        for sh in ("g", "h"):
+            alpha = float(np.exp(rng.uniform(np.log(0.3), np.log(3.0))))
+            for t in synth.SHELL_TYPES[sh]:
+                ic.append(a + 1)
+                it.append(t)
+                e.append(alpha)
+    extra = len(e) - mol.npri
+    cmo = np.concatenate([mol.cmo, 0.3 * rng.standard_normal((extra, mol.nmo))])
+    return synth.Molecule(mol.atom_xyz, mol.atom_z, np.array(ic, np.int32), np.array(it, np.int32),
+                          np.array(e), mol.occ, np.ascontiguousarray(cmo), name="nci12gh")
+
+
+def test_g_and_h_shells(gpu_lib, oracle_mod):
+    """g and h primitives (critic2's li rows 21-56): FP64 rho2 against the
+    oracle (whose g/h chi are pinned symbolically)."""
+    from critic2_gb300.wfn import Wavefunction
+    m = gh_molecule()
+    g, o = Wavefunction(m), oracle_mod.Wfn(m)
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(m.atom_xyz.min(0) - 1, m.atom_xyz.max(0) + 1, size=(80, 3))
+    out = g.rho2(pts, 2, "fp64")
+    for i in range(80):
+        ref = o.rho2(pts[i], 2)
+        assert close(out["rho"][i], ref["rho"])
+        assert close(out["grad"][i], ref["grad"])
+        assert close(out["hess"][i], ref["h"])

@@ -164,3 +164,24 @@ def test_autocritic_split_same_cps(w12, o12):
     assert len(unmatched(ref, res)) <= max(1, len(ref["xyz"]) // 50)
     print(f"\nAUTO nci12: fp64 {ref['counts']} ph {ref['ph']} ({ref['ms']:.0f} ms), "
           f"tf32x3 {res['counts']} ph {res['ph']} ({res['ms']:.0f} ms)")
+
+
+def test_g_and_h_shells_split():
+    """Split precision with g and h primitives (the general-l producer paths:
+    point lists and the separable-brick grid path) against FP64."""
+    from test_gpu_fp64 import gh_molecule
+    from critic2_gb300.wfn import Wavefunction
+    m = gh_molecule()
+    w = Wavefunction(m)
+    x0, xm, ns = synth.nci_grid(m, 40, 0.15)
+    c64, g64, _ = w.nciplot(x0, xm, ns, "fp64")
+    rng = np.random.default_rng(2)
+    pts = rng.uniform(m.atom_xyz.min(0), m.atom_xyz.max(0), size=(500, 3))
+    r64 = w.rho2(pts, 2, "fp64")
+    for prec in ("tf32x3", "bf16x3"):
+        c, s, _ = w.nciplot(x0, xm, ns, prec)
+        rho, rho64 = np.abs(c) / 100, np.abs(c64) / 100
+        assert np.max(np.abs(rho - rho64) / rho64) < TOL[prec]["rho"]
+        assert np.max(np.abs(s - g64)) < TOL[prec]["s"]
+        r = w.rho2(pts, 2, prec)
+        assert np.max(np.abs(r["rho"][:, 0] - r64["rho"][:, 0]) / r64["rho"][:, 0]) < TOL[prec]["rho"]

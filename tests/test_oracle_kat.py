@@ -2,8 +2,8 @@
 
 The reference cannot be run here, so the evaluator restatement is pinned by
 mathematics: (1) exact symbolic density, gradient and Hessian of small
-wavefunctions (sympy), covering every Cartesian type s..f of critic2's li
-table; (2) normalisation integrals of normalised primitives by Gauss-Hermite
+wavefunctions (sympy), covering every Cartesian type s..h of critic2's li
+table (types 1-56); (2) normalisation integrals of normalised primitives by Gauss-Hermite
 quadrature (exact for polynomial x Gaussian), which pins the exponent
 convention exp(-alpha r^2) and the coefficient layout; (3) finite
 differences on a synthetic workload molecule; (4) the primitive cutoff
@@ -46,7 +46,7 @@ def sym_density(mol):
 
 
 @pytest.mark.parametrize("types", [[1], [2, 3, 4], list(range(5, 11)), list(range(11, 21)),
-                                   [1, 2, 7, 9, 12, 20]])
+                                   [1, 2, 7, 9, 12, 20], list(range(21, 36)), list(range(36, 57))])
 def test_symbolic_density(oracle_mod, types):
     rng = np.random.default_rng(len(types))
     n = len(types)
