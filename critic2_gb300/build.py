@@ -44,8 +44,9 @@ def _stale(objs) -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
-    deps.append(os.path.join(HERE, "..", "include", "critic2_gb300.h"))
+    deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    inc = os.path.join(HERE, "..", "include")
+    deps += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 

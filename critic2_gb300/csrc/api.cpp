@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <numeric>
 #include <stdexcept>
 #include <string>
 
@@ -106,6 +107,65 @@ void build_device(Handle &h) {
   d.wup = d.spin ? upload(h, wup) : nullptr;
   d.wdn = d.spin ? upload(h, wdn) : nullptr;
   for (int j = 0; j < 3; j++) d.cell_lo[j] = w.cell_lo[j], d.cell_aa[j] = w.cell_aa[j];
+  d.edf = nullptr;
+  d.nedf = 0;
+}
+
+// Uploads the EDF core primitives in centre-major order (critic2's
+// icord_edf, src/wfn_private@proc.F90:3758-3776) and refreshes the atoms'
+// spcutoff^2, which the EDF cutoffs widen.
+void upload_edf(Handle &h) {
+  HostWfn &w = h.host;
+  DevWfn &d = h.dev;
+  std::vector<double4> atoms(w.natom);
+  for (int a = 0; a < w.natom; a++)
+    atoms[a] = make_double4(w.xyz[3 * a], w.xyz[3 * a + 1], w.xyz[3 * a + 2],
+                            w.spcutoff[a] * w.spcutoff[a]);
+  C2G_CUDA(cudaMemcpy(const_cast<double4 *>(d.atoms), atoms.data(), sizeof(double4) * w.natom,
+                      cudaMemcpyHostToDevice));
+  if (h.edf_buf) {
+    C2G_CUDA(cudaFree(h.edf_buf));
+    h.edf_buf = nullptr;
+  }
+  d.edf = nullptr;
+  d.nedf = 0;
+  if (w.nedf == 0) return;
+  std::vector<int> ord(w.nedf);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(),
+                   [&](int a, int b) { return w.edf_icenter[a] < w.edf_icenter[b]; });
+  std::vector<PrimEDF> prim(w.nedf);
+  for (int k = 0; k < w.nedf; k++) {
+    const int i = ord[k];
+    const int *l = kLi[w.edf_itype[i] - 1];
+    prim[k] = PrimEDF{w.edf_e[i], w.edf_dran[i], w.edf_c[i], l[0] | (l[1] << 4) | (l[2] << 8),
+                      w.edf_icenter[i]};
+  }
+  C2G_CUDA(cudaMalloc(&h.edf_buf, sizeof(PrimEDF) * prim.size()));
+  C2G_CUDA(cudaMemcpy(h.edf_buf, prim.data(), sizeof(PrimEDF) * prim.size(), cudaMemcpyHostToDevice));
+  d.edf = static_cast<const PrimEDF *>(h.edf_buf);
+  d.nedf = w.nedf;
+}
+
+// Replaces the EDF core of a handle (host arrays, cutoffs, device copy).
+void set_edf(Handle &h, int nedf, const int *icenter, const int *itype, const double *e, const double *c) {
+  HostWfn &w = h.host;
+  require(nedf >= 0, "nedf must be non-negative");
+  require(nedf == 0 || (icenter && itype && e && c), "null EDF array");
+  for (int i = 0; i < nedf; i++) {
+    require(icenter[i] >= 1 && icenter[i] <= w.natom, "EDF icenter out of range");
+    require(itype[i] >= 1 && itype[i] <= 56, "EDF itype out of range (1..56)");
+    require(e[i] > 0.0, "EDF exponents must be positive");
+  }
+  w.nedf = nedf;
+  w.edf_icenter.resize(nedf);
+  for (int i = 0; i < nedf; i++) w.edf_icenter[i] = icenter[i] - 1;
+  w.edf_itype.assign(itype, itype + nedf);
+  w.edf_e.assign(e, e + nedf);
+  w.edf_c.assign(c, c + nedf);
+  complete_struct(w);
+  DeviceGuard g(h.device);
+  upload_edf(h);
 }
 
 Handle *check_handle(c2g_wfn *hp) {
@@ -344,6 +404,18 @@ int c2g_wfn_read_wfx(const char *path, c2g_wfn **out) {
                             w.itype.data(), w.e.data(), w.occ.data(), w.cmo.data(), w.wfntyp,
                             w.nalpha, out);
     if (rc != C2G_OK) fail(rc, g_last_error);
+    if (w.nedf > 0) {
+      std::vector<int> ic(w.nedf);
+      for (int i = 0; i < w.nedf; i++) ic[i] = w.edf_icenter[i] + 1;
+      try {
+        set_edf(*reinterpret_cast<Handle *>(*out), w.nedf, ic.data(), w.edf_itype.data(), w.edf_e.data(),
+                w.edf_c.data());
+      } catch (...) {
+        c2g_wfn_destroy(*out);
+        *out = nullptr;
+        throw;
+      }
+    }
   });
 }
 
@@ -355,9 +427,15 @@ int c2g_wfn_destroy(c2g_wfn *hp) {
       DeviceGuard g(h->device);
       if (h->tc) tc_destroy(h->tc);
       for (void *p : h->allocations) cudaFree(p);
+      if (h->edf_buf) cudaFree(h->edf_buf);
     }
     delete h;
   });
+}
+
+int c2g_wfn_set_edf(c2g_wfn *hp, int nedf, const int *icenter, const int *itype, const double *e,
+                    const double *c) {
+  return guarded([&] { set_edf(*check_handle(hp), nedf, icenter, itype, e, c); });
 }
 
 int c2g_wfn_set_param(c2g_wfn *hp, int param, double value) {

@@ -60,6 +60,11 @@ struct HostWfn {
   std::vector<int> lmax;        // natom
   std::vector<int> icord;       // npri: primitives ordered by centre
   std::vector<int> iprilo, iprihi;  // natom, ranges in icord
+  // EDF core density (nedf = 0 without one), in input order
+  int nedf = 0;
+  std::vector<int> edf_icenter;  // nedf, 0-based
+  std::vector<int> edf_itype;    // nedf, 1-based li index
+  std::vector<double> edf_e, edf_c, edf_dran;
   // molecular cell (bounding box grown by the 10 angstrom border)
   double cell_lo[3], cell_aa[3], molborder[3];
 };
@@ -82,6 +87,15 @@ struct __align__(16) PrimF64 {
   int pad0, pad1;
 };
 
+// An EDF core primitive (centre-major order).
+struct __align__(16) PrimEDF {
+  double e;      // exponent
+  double dran;   // cutoff distance sqrt(-ln(1e-12)/e)
+  double c;      // coefficient
+  int lpack;     // lx | ly << 4 | lz << 8
+  int atom;      // 0-based centre
+};
+
 struct DevWfn {
   int natom, npri, nmo, nmo_pad;
   const double4 *atoms;   // x, y, z, spcutoff^2
@@ -93,6 +107,8 @@ struct DevWfn {
   const double *wdn;
   double cell_lo[3], cell_aa[3];
   int spin;               // 1 for UHF/ROHF
+  const PrimEDF *edf;     // nedf core primitives, or null
+  int nedf;
 };
 
 struct TcOperands;  // split-precision operands (k_tc.cu)
@@ -104,6 +120,7 @@ struct Handle {
   std::vector<void *> allocations;
   TcOperands *tc = nullptr;
   int newton_stall = 0;  // C2G_PARAM_NEWTON_STALL (0: critic2's maxit only)
+  void *edf_buf = nullptr;  // device EDF primitives (replaced by c2g_wfn_set_edf)
 };
 
 // per-point record produced by the evaluator (FP64 path), quantities:

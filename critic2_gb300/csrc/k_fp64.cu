@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "c2g_internal.h"
+#include "gto.cuh"
 #include "points.cuh"
 
 namespace c2g {
@@ -30,47 +31,6 @@ constexpr int NG = 8;      // MO groups = warps
 constexpr int KCH = 8;     // primitives per chunk (one per warp)
 constexpr int NTHR = TP * NG;
 constexpr int kPointKernelMax = 65536;  // index batches up to this size use k_eval_fp64_pt
-
-// x^l factors of one Cartesian axis and their first and second derivatives
-// including the Gaussian's exp(-al r^2) chain rule:
-//   f0 = x^l, f1 = l x^(l-1) - 2 al x^(l+1),
-//   f2 = l(l-1) x^(l-2) - 2 al (2l+1) x^l + 4 al^2 x^(l+2).
-__device__ __forceinline__ void axis_factors(double x, int l, double al, double &f0, double &f1,
-                                             double &f2) {
-  double a = 1.0, b = 0.0, c = 0.0;  // x^l, x^(l-1), x^(l-2)
-  for (int i = 0; i < l; i++) {
-    c = b;
-    b = a;
-    a *= x;
-  }
-  const double p1 = a * x, p2 = p1 * x;
-  f0 = a;
-  f1 = l * b - 2.0 * al * p1;
-  f2 = (double)(l * (l - 1)) * c - 2.0 * al * (double)(2 * l + 1) * a + 4.0 * al * al * p2;
-}
-
-template <int NC>
-__device__ __forceinline__ void chi_eval(double dx, double dy, double dz, double al, int lpack,
-                                         double ex, double (&chi)[NC]) {
-  double fx0, fx1, fx2, fy0, fy1, fy2, fz0, fz1, fz2;
-  axis_factors(dx, lpack & 15, al, fx0, fx1, fx2);
-  axis_factors(dy, (lpack >> 4) & 15, al, fy0, fy1, fy2);
-  axis_factors(dz, (lpack >> 8) & 15, al, fz0, fz1, fz2);
-  chi[0] = fx0 * fy0 * fz0 * ex;
-  if constexpr (NC > 1) {
-    chi[1] = fx1 * fy0 * fz0 * ex;
-    chi[2] = fy1 * fx0 * fz0 * ex;
-    chi[3] = fz1 * fx0 * fy0 * ex;
-  }
-  if constexpr (NC > 4) {
-    chi[4] = fx2 * fy0 * fz0 * ex;
-    chi[5] = fy2 * fz0 * fx0 * ex;
-    chi[6] = fz2 * fx0 * fy0 * ex;
-    chi[7] = fx1 * fy1 * fz0 * ex;
-    chi[8] = fx1 * fz1 * fy0 * ex;
-    chi[9] = fz1 * fy1 * fx0 * ex;
-  }
-}
 
 // ------------------------------------------------------------------ sinks
 struct RecSink {
@@ -201,6 +161,11 @@ __device__ __forceinline__ void point_record(const double (&acc)[MPG][NC], const
         }
       }
     }
+    if constexpr (NC == 1 && NR > kRecNci && SPIN) {
+      // density only (nder = 0): the spin channels' rho
+#pragma unroll
+      for (int s = 0; s < 2; s++) r[17 + 11 * s] += (s == 0 ? w.wup : w.wdn)[mo0 + m] * p0 * p0;
+    }
   }
 }
 
@@ -309,6 +274,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_eval_fp64(DevWfn w, Src src, Sink s
     }
     if (tid < TP && s_valid[tid]) {
       const double x[3] = {s_x[0][tid], s_x[1][tid], s_x[2][tid]};
+      if (w.nedf) edf_add_record(w, x, s_acc + tid, TP, NR, SPIN);
       sink.put(w, s_idx[tid], x, s_acc + tid, TP);
     }
     __syncthreads();
@@ -416,10 +382,20 @@ __global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, IndexSrc src, do
 #pragma unroll
     for (int q = 0; q < kRecNci; q++) s_red[wp * kRecNci + q] = r[q];
   __syncthreads();
-  if (tid < kRecNci) {
-    double sum = 0.0;
-    for (int i = 0; i < 8; i++) sum += s_red[i * kRecNci + tid];
-    rec[idx * kRecNci + tid] = sum;
+  if (wp == 0) {
+    double core_q = 0.0;  // EDF core, component `lane`
+    if (w.nedf) {
+      double core[10];
+      edf_core_warp(w, x, core);
+#pragma unroll
+      for (int q = 0; q < 10; q++)
+        if (q == lane) core_q = core[q];
+    }
+    if (tid < kRecNci) {
+      double sum = 0.0;
+      for (int i = 0; i < 8; i++) sum += s_red[i * kRecNci + tid];
+      rec[idx * kRecNci + tid] = sum + core_q;
+    }
   }
 }
 

@@ -44,6 +44,7 @@
 #include <numeric>
 #include <vector>
 
+#include "gto.cuh"
 #include "k_tc.h"
 #include "points.cuh"
 #include "ptx_sm100.h"
@@ -712,6 +713,23 @@ struct TcNciSink {
   }
 };
 
+// Hands a point's 10 valence sums to the sink, with the EDF core (FP64,
+// gto.cuh) added first when the wavefunction has one.
+template <class Sink, class T>
+__device__ __forceinline__ void put_point(const TcArgs &a, const Sink &sink, long idx, const T *v, int stride,
+                                          const double *xp) {
+  if (a.w.nedf) {
+    const double x[3] = {xp[0], xp[1], xp[2]};
+    double r[10];
+    edf_core(a.w, x, r);
+#pragma unroll
+    for (int k = 0; k < 10; k++) r[k] += (double)v[k * stride];
+    sink.put(a, idx, r, 1);
+  } else {
+    sink.put(a, idx, v, stride);
+  }
+}
+
 // ------------------------------------------------------------------ kernel
 template <int KIND, class Src, class Sink>
 __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink, int ntiles) {
@@ -1057,13 +1075,14 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
             v4[k] = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
           }
           const long idx = s.idx[par * 32 + p];
+          const double *xp = s.x + (par * 32 + p) * 3;
           if (a.nmt == 1) {
-            if (idx >= 0) sink.put(a, idx, v4, 1);
+            if (idx >= 0) put_point(a, sink, idx, v4, 1, xp);
           } else {
 #pragma unroll
             for (int k = 0; k < 10; k++) s.acc[k * 32 + p] += (double)v4[k];
             if (mt == a.nmt - 1) {
-              if (idx >= 0) sink.put(a, idx, s.acc + p, 32);
+              if (idx >= 0) put_point(a, sink, idx, s.acc + p, 32, xp);
 #pragma unroll
               for (int k = 0; k < 10; k++) s.acc[k * 32 + p] = 0.0;
             }

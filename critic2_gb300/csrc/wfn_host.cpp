@@ -95,6 +95,13 @@ void complete_struct(HostWfn &w) {
     if (!seen[a]) w.iprilo[a] = k, seen[a] = 1;
     w.iprihi[a] = k;
   }
+  // EDF cutoffs widen the atoms' environment radius (:3750-3756)
+  w.edf_dran.assign(w.nedf, 0.0);
+  for (int i = 0; i < w.nedf; i++) {
+    w.edf_dran[i] = std::sqrt(-std::log(kPrimThreshold) / w.edf_e[i]);
+    const int a = w.edf_icenter[i];
+    w.spcutoff[a] = std::max(w.spcutoff[a], w.edf_dran[i]);
+  }
 }
 
 void molecular_cell(HostWfn &w) {
@@ -174,7 +181,6 @@ bool read_wfx(const char *path, HostWfn &w, std::string &err) {
   if (nmo <= 0) { err = "Number of Occupied Molecular Orbitals tag not found"; return false; }
   if (npri <= 0) { err = "Number of Primitives tag not found"; return false; }
   if (nat <= 0) { err = "Number of Nuclei tag not found"; return false; }
-  if (nedf > 0) { err = "EDF core densities are not supported"; return false; }
   in.clear();
   in.seekg(0);
   w = HostWfn();
@@ -182,9 +188,11 @@ bool read_wfx(const char *path, HostWfn &w, std::string &err) {
   w.npri = npri;
   w.nmo = nmo;
   w.cmo.assign((size_t)npri * nmo, 0.0);
+  w.nedf = std::max(nedf, 0);
   std::vector<double> buf;
   bool have_xyz = false, have_z = false, have_c = false, have_t = false, have_e = false,
        have_o = false, have_mo = false;
+  int have_edf = 0;  // bit per EDF section: centres, types, exponents, coefficients
   while (std::getline(in, line)) {
     std::string t = trim(line);
     if (t.size() < 2 || t[0] != '<' || t[1] == '/') continue;
@@ -225,7 +233,32 @@ bool read_wfx(const char *path, HostWfn &w, std::string &err) {
         for (int i = 0; i < npri; i++) w.cmo[(size_t)i * nmo + m] = buf[i];
       }
       have_mo = true;
+    } else if (w.nedf > 0 && t == "<EDF Primitive Centers>") {
+      if (!read_block(in, buf, w.nedf, nullptr)) { err = "bad <EDF Primitive Centers>"; return false; }
+      w.edf_icenter.resize(w.nedf);
+      for (int i = 0; i < w.nedf; i++) w.edf_icenter[i] = (int)buf[i] - 1;
+      have_edf |= 1;
+    } else if (w.nedf > 0 && t == "<EDF Primitive Types>") {
+      if (!read_block(in, buf, w.nedf, nullptr)) { err = "bad <EDF Primitive Types>"; return false; }
+      w.edf_itype.assign(buf.begin(), buf.end());
+      for (int v : w.edf_itype)
+        if (v < 1 || v > 56) { err = "primitive type not supported"; return false; }
+      have_edf |= 2;
+    } else if (w.nedf > 0 && t == "<EDF Primitive Exponents>") {
+      if (!read_block(in, w.edf_e, w.nedf, nullptr)) { err = "bad <EDF Primitive Exponents>"; return false; }
+      have_edf |= 4;
+    } else if (w.nedf > 0 && t == "<EDF Primitive Coefficients>") {
+      if (!read_block(in, w.edf_c, w.nedf, nullptr)) { err = "bad <EDF Primitive Coefficients>"; return false; }
+      have_edf |= 8;
     }
+  }
+  if (w.nedf > 0 && have_edf != 15) {
+    err = "wfx file is missing an EDF section";
+    return false;
+  }
+  for (int i = 0; i < w.nedf; i++) {
+    if (w.edf_icenter[i] < 0 || w.edf_icenter[i] >= nat) { err = "EDF primitive centre out of range"; return false; }
+    if (!(w.edf_e[i] > 0.0)) { err = "EDF exponents must be positive"; return false; }
   }
   if (!(have_xyz && have_z && have_c && have_t && have_e && have_o && have_mo)) {
     err = "wfx file is missing a required section";

@@ -95,6 +95,15 @@ class Molecule:
     wfntyp: int = 0          # 0 rhf, 1 uhf, 2 rohf, 3 frac
     nalpha: int = 0
     name: str = ""
+    # EDF core density (wfx <EDF Primitive *> sections), None without one
+    edf_icenter: Optional[np.ndarray] = None  # (nedf,) int32, 1-based
+    edf_itype: Optional[np.ndarray] = None    # (nedf,) int32, 1-based li index
+    edf_e: Optional[np.ndarray] = None        # (nedf,) float64
+    edf_c: Optional[np.ndarray] = None        # (nedf,) float64
+
+    @property
+    def nedf(self) -> int:
+        return 0 if self.edf_e is None else int(self.edf_e.shape[0])
 
     @property
     def natom(self) -> int:
@@ -204,6 +213,35 @@ def build_molecule(w: Workload, seed: int) -> Molecule:
                     wfntyp=0, nalpha=w.nmo, name=w.name)
 
 
+def add_edf(mol: Molecule, seed: int, per_atom=(3, 6), lmax: int = 0) -> Molecule:
+    """Returns a copy of `mol` with a seeded synthetic EDF core on every
+    heavy atom: `per_atom` s-type primitives with exponents 2-2000 and
+    positive coefficients (a compact core density, as the EDFs that stand in
+    for pseudopotential cores), plus, for lmax >= 1, one primitive of each
+    type up to lmax with small signed coefficients (types beyond s exercise
+    the full polynomial; they stay within the atom's MO lmax)."""
+    rng = np.random.default_rng(seed)
+    ic, it, ee, cc = [], [], [], []
+    for a in range(mol.natom):
+        if int(mol.atom_z[a]) == 1:
+            continue
+        for _ in range(int(rng.integers(per_atom[0], per_atom[1] + 1))):
+            ic.append(a + 1)
+            it.append(1)
+            ee.append(math.exp(rng.uniform(math.log(2.0), math.log(2000.0))))
+            cc.append(math.exp(rng.uniform(math.log(0.5), math.log(200.0))))
+        for t in range(2, 57):
+            if max(LI[t - 1]) > lmax:
+                continue
+            ic.append(a + 1)
+            it.append(t)
+            ee.append(math.exp(rng.uniform(math.log(1.0), math.log(50.0))))
+            cc.append(float(rng.uniform(-1.0, 1.0)))
+    return dataclasses.replace(mol, edf_icenter=np.array(ic, np.int32), edf_itype=np.array(it, np.int32),
+                               edf_e=np.array(ee, np.float64), edf_c=np.array(cc, np.float64),
+                               name=mol.name + "+edf")
+
+
 def nci_grid(mol: Molecule, n: int, step: float):
     """NCI grid geometry in critic2's form (src/nci@proc.f90:430-447).
 
@@ -288,5 +326,11 @@ def write_wfx(mol: Molecule, path: str) -> None:
         for i in range(0, mol.npri, 4):
             out.append(" " + " ".join(f"{v: .16E}" for v in col[i:i + 4]))
     out.append("</Molecular Orbital Primitive Coefficients>")
+    if mol.nedf:
+        out += ["<Number of EDF Primitives>", f" {mol.nedf}", "</Number of EDF Primitives>"]
+        out += block("EDF Primitive Centers", [int(v) for v in mol.edf_icenter], lambda v: f"{v:d}")
+        out += block("EDF Primitive Types", [int(v) for v in mol.edf_itype], lambda v: f"{v:d}")
+        out += block("EDF Primitive Exponents", [float(v) for v in mol.edf_e], lambda v: f"{v:.16E}")
+        out += block("EDF Primitive Coefficients", [float(v) for v in mol.edf_c], lambda v: f"{v:.16E}")
     with open(path, "w") as fh:
         fh.write("\n".join(out) + "\n")

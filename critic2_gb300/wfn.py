@@ -46,6 +46,8 @@ class Wavefunction:
                 mol.natom, _f64(mol.atom_xyz.reshape(-1)), _i32(mol.atom_z), mol.npri, mol.nmo,
                 _i32(mol.icenter), _i32(mol.itype), _f64(mol.e), _f64(mol.occ),
                 _f64(mol.cmo.reshape(-1)), int(mol.wfntyp), int(mol.nalpha), C.byref(self._h)))
+        if mol is not None and mol.nedf:
+            self.set_edf(mol.edf_icenter, mol.edf_itype, mol.edf_e, mol.edf_c)
         n = [C.c_int() for _ in range(5)]
         L.check(L.lib().c2g_wfn_info(self._h, *[C.byref(v) for v in n]))
         self.natom, self.npri, self.nmo, self.wfntyp, self.nalpha = (v.value for v in n)
@@ -72,6 +74,14 @@ class Wavefunction:
 
     def __exit__(self, *a):
         self.close()
+
+    def set_edf(self, icenter, itype, e, c):
+        """EDF core density (c2g_wfn_set_edf): 1-based centres and li types,
+        exponents and coefficients; empty arrays remove the core."""
+        ic, it, ee, cc = _i32(icenter), _i32(itype), _f64(e), _f64(c)
+        n = int(ee.shape[0])
+        L.check(L.lib().c2g_wfn_set_edf(self._h, n, L.ptr(ic) if n else None, L.ptr(it) if n else None,
+                                        L.ptr(ee) if n else None, L.ptr(cc) if n else None))
 
     def set_recheck(self, rel: float):
         """Relative |lambda2| below which split-precision NCI points are

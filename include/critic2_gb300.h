@@ -90,6 +90,25 @@ int c2g_wfn_read_wfx(const char *path, c2g_wfn **out);
 /* Frees the handle and its device memory. */
 int c2g_wfn_destroy(c2g_wfn *h);
 
+/* Sets (or, with nedf = 0, removes) the EDF core density of a handle: the
+ * electron density functions of pseudopotential cores, a linear sum
+ * sum_i c(i) chi_i(r) of Cartesian Gaussians added to the MO density in
+ * every evaluation (total density, and half of it to each spin channel of
+ * a UHF/ROHF wavefunction; kinetic energy density and stress have no core
+ * part).  Arrays as in the wfx <EDF Primitive *> sections:
+ *   icenter(nedf), itype(nedf): 1-based centre and li type (1..56)
+ *   e(nedf): exponents, c(nedf): coefficients
+ * The cutoffs are critic2's: dran_edf = sqrt(-ln(1e-12)/e), and each atom's
+ * environment radius grows to cover its EDF primitives.  c2g_wfn_read_wfx
+ * calls this for files with <Number of EDF Primitives> > 0.  Replaces the
+ * EDF part of read_wfx and complete_struct and calculate_edf
+ * (src/wfn_private@proc.F90:1185-1230, 3750-3776, 3275-3369, 2626-2677);
+ * critic2 builds the EDF polynomial powers only up to the atom's MO lmax
+ * (s-type EDFs, the usual case, are unaffected), this library evaluates the
+ * full polynomial of every type. */
+int c2g_wfn_set_edf(c2g_wfn *h, int nedf, const int *icenter, const int *itype, const double *e,
+                    const double *c);
+
 /* Tunable parameters of a handle. */
 #define C2G_PARAM_RECHECK_REL 1 /* split-precision NCI: points with
                                    |lambda2| < value * max|lambda| are

@@ -47,6 +47,11 @@ struct owfn {
   double *dran, *spcutoff;
   int *lmax, *icord, *iprilo, *iprihi;
   double cell_lo[3], aa[3], molborder[3];
+  /* EDF core (src/wfn_private.f90 molwfn: nedf, icenter_edf, itype_edf,
+   * e_edf, c_edf, dran_edf, icord_edf, iprilo_edf, iprihi_edf) */
+  int nedf;
+  int *icenter_edf, *itype_edf, *icord_edf, *iprilo_edf, *iprihi_edf;
+  double *e_edf, *c_edf, *dran_edf;
 };
 
 static int limax_of(int itype) {
@@ -188,12 +193,64 @@ owfn *o_wfn_new(int natom, const double *xyz, const int *z, int npri, int nmo,
   return w;
 }
 
+static void free_edf(owfn *w) {
+  free(w->icenter_edf); free(w->itype_edf); free(w->icord_edf); free(w->iprilo_edf);
+  free(w->iprihi_edf); free(w->e_edf); free(w->c_edf); free(w->dran_edf);
+  w->icenter_edf = w->itype_edf = w->icord_edf = w->iprilo_edf = w->iprihi_edf = NULL;
+  w->e_edf = w->c_edf = w->dran_edf = NULL;
+  w->nedf = 0;
+}
+
 void o_wfn_free(owfn *w) {
   if (!w) return;
   free(w->xyz); free(w->z); free(w->icenter); free(w->itype); free(w->e);
   free(w->occ); free(w->cmo); free(w->dran); free(w->spcutoff); free(w->lmax);
   free(w->icord); free(w->iprilo); free(w->iprihi);
+  free_edf(w);
   free(w);
+}
+
+/* The EDF part of read_wfx + complete_struct (src/wfn_private@proc.F90:
+ * 1185-1230, 3750-3776): dran_edf = sqrt(-ln(thres)/alpha), the atom's
+ * spcutoff grows to cover its EDF primitives, EDF primitives ordered by
+ * centre.  EDF primitives are not pruned.  icenter is 1-based.  nedf = 0
+ * removes the core; the MO cutoffs are recomputed from scratch. */
+void o_wfn_set_edf(owfn *w, int nedf, const int *icenter, const int *itype, const double *e,
+                   const double *c) {
+  free_edf(w);
+  free(w->dran); free(w->spcutoff); free(w->lmax); free(w->icord); free(w->iprilo); free(w->iprihi);
+  complete_struct(w);
+  if (nedf <= 0) return;
+  int na = w->natom;
+  w->nedf = nedf;
+  w->icenter_edf = malloc(sizeof(int) * nedf);
+  w->itype_edf = malloc(sizeof(int) * nedf);
+  w->e_edf = malloc(sizeof(double) * nedf);
+  w->c_edf = malloc(sizeof(double) * nedf);
+  w->dran_edf = malloc(sizeof(double) * nedf);
+  w->icord_edf = malloc(sizeof(int) * nedf);
+  w->iprilo_edf = malloc(sizeof(int) * na);
+  w->iprihi_edf = malloc(sizeof(int) * na);
+  for (int i = 0; i < nedf; i++) {
+    w->icenter_edf[i] = icenter[i] - 1;
+    w->itype_edf[i] = itype[i];
+    w->e_edf[i] = e[i];
+    w->c_edf[i] = c[i];
+    w->dran_edf[i] = sqrt(-log(RPRIM_THRES) / e[i]);
+    int a = w->icenter_edf[i];
+    if (w->dran_edf[i] > w->spcutoff[a]) w->spcutoff[a] = w->dran_edf[i];
+  }
+  int k = 0;
+  for (int a = 0; a < na; a++) {
+    w->iprilo_edf[a] = -1;
+    w->iprihi_edf[a] = -2;
+    for (int i = 0; i < nedf; i++)
+      if (w->icenter_edf[i] == a) {
+        if (w->iprilo_edf[a] < 0) w->iprilo_edf[a] = k;
+        w->iprihi_edf[a] = k;
+        w->icord_edf[k++] = i;
+      }
+  }
 }
 
 int o_wfn_npri(const owfn *w) { return w->npri; }
@@ -277,7 +334,67 @@ static void calculate_mo_gto(const owfn *w, const double xpos[3], int nder, doub
   }
 }
 
-/* molwfn%rho2, src/wfn_private@proc.F90:2484-2705 (no EDF core). Output
+/* calculate_edf, src/wfn_private@proc.F90:3275-3369: the core density
+ * rhoc = sum c_edf chi over the EDF primitives of the environment's atoms
+ * (d^2 <= spcutoff^2) with dist <= dran_edf, its gradient and Hessian
+ * hc = (xx, yy, zz, xy, xz, yz).  The reference tabulates the powers x^l
+ * only up to the atom's MO lmax; here they are tabulated up to 5, which is
+ * the same for every EDF type within lmax (s-type EDFs always are). */
+static void calculate_edf(const owfn *w, const double xpos[3], int nder, double *rhoc, double gradc[3],
+                          double hc[6]) {
+  *rhoc = 0.0;
+  for (int j = 0; j < 3; j++) gradc[j] = 0.0;
+  for (int j = 0; j < 6; j++) hc[j] = 0.0;
+  if (w->nedf == 0) return;
+  for (int a = 0; a < w->natom; a++) {
+    double xx[3], dd = 0.0;
+    for (int j = 0; j < 3; j++) {
+      xx[j] = xpos[j] - w->xyz[3 * a + j];
+      dd += xx[j] * xx[j];
+    }
+    if (!(dd <= w->spcutoff[a] * w->spcutoff[a])) continue;
+    if (w->iprilo_edf[a] < 0) continue;
+    double dist = sqrt(dd), d2 = dist * dist;
+    double xl[3][3][6];
+    for (int ix = 0; ix < 3; ix++) {
+      xl[ix][0][0] = 1.0; xl[ix][1][0] = 0.0; xl[ix][2][0] = 0.0;
+      xl[ix][0][1] = xx[ix]; xl[ix][1][1] = 1.0; xl[ix][2][1] = 0.0;
+      for (int l = 2; l <= 5; l++) {
+        xl[ix][0][l] = xl[ix][0][l - 1] * xx[ix];
+        xl[ix][1][l] = l * xl[ix][0][l - 1];
+        xl[ix][2][l] = l * (l - 1) * xl[ix][0][l - 2];
+      }
+    }
+    for (int j = w->iprilo_edf[a]; j <= w->iprihi_edf[a]; j++) {
+      int ip = w->icord_edf[j];
+      if (dist > w->dran_edf[ip]) continue;
+      const int *l = LI[w->itype_edf[ip] - 1];
+      double al = w->e_edf[ip];
+      double ex = exp(-al * d2);
+      double exc = w->c_edf[ip] * ex;
+      *rhoc += w->c_edf[ip] * xl[0][0][l[0]] * xl[1][0][l[1]] * xl[2][0][l[2]] * ex;
+      if (nder < 1) continue;
+      double f1x = xl[0][1][l[0]] - 2 * al * ipow(xx[0], l[0] + 1);
+      double f1y = xl[1][1][l[1]] - 2 * al * ipow(xx[1], l[1] + 1);
+      double f1z = xl[2][1][l[2]] - 2 * al * ipow(xx[2], l[2] + 1);
+      gradc[0] += f1x * xl[1][0][l[1]] * xl[2][0][l[2]] * exc;
+      gradc[1] += f1y * xl[0][0][l[0]] * xl[2][0][l[2]] * exc;
+      gradc[2] += f1z * xl[0][0][l[0]] * xl[1][0][l[1]] * exc;
+      if (nder < 2) continue;
+      hc[0] += (xl[0][2][l[0]] - 2 * al * (2 * l[0] + 1) * xl[0][0][l[0]] + 4 * al * al * ipow(xx[0], l[0] + 2)) *
+               xl[1][0][l[1]] * xl[2][0][l[2]] * exc;
+      hc[1] += (xl[1][2][l[1]] - 2 * al * (2 * l[1] + 1) * xl[1][0][l[1]] + 4 * al * al * ipow(xx[1], l[1] + 2)) *
+               xl[2][0][l[2]] * xl[0][0][l[0]] * exc;
+      hc[2] += (xl[2][2][l[2]] - 2 * al * (2 * l[2] + 1) * xl[2][0][l[2]] + 4 * al * al * ipow(xx[2], l[2] + 2)) *
+               xl[0][0][l[0]] * xl[1][0][l[1]] * exc;
+      hc[3] += f1x * f1y * xl[2][0][l[2]] * exc;
+      hc[4] += f1x * f1z * xl[1][0][l[1]] * exc;
+      hc[5] += f1z * f1y * xl[0][0][l[0]] * exc;
+    }
+  }
+}
+
+/* molwfn%rho2, src/wfn_private@proc.F90:2484-2705. Output
  * arrays are Fortran-ordered: rho(3) = total/up/down, grad(3,3) column j =
  * spin j, h(3,3,3) column-major per spin, stress(3,3). */
 void o_rho2(const owfn *w, const double xpos[3], int nder, double rho[3], double rhoval[3],
@@ -334,17 +451,23 @@ void o_rho2(const owfn *w, const double xpos[3], int nder, double rho[3], double
     }
   }
   free(phi);
-  /* core density contribution is zero (nedf = 0) */
+  /* core contribution (:2626-2677): RHF-like types add it to the total and
+   * halve; UHF/ROHF add it to the total and half to each spin channel */
+  double rhoc, gradc[3], hhc[6];
+  calculate_edf(w, xpos, nder, &rhoc, gradc, hhc);
   if (!uhf && !rohf) {
     rhoval[0] = rh[0]; rhoval[1] = 0.5 * rh[0]; rhoval[2] = rhoval[1];
+    rh[0] += rhoc;
     rh[1] = 0.5 * rh[0]; rh[2] = rh[1];
     for (int j = 0; j < 3; j++) {
       gradval[j] = g[0][j]; gradval[3 + j] = 0.5 * g[0][j]; gradval[6 + j] = 0.5 * g[0][j];
+      g[0][j] += gradc[j];
       g[1][j] = 0.5 * g[0][j]; g[2][j] = g[1][j];
     }
     gk[1] = gk[0] / 2; gk[2] = gk[1];
     for (int j = 0; j < 6; j++) {
       hhval[0][j] = hh[0][j]; hhval[1][j] = 0.5 * hh[0][j]; hhval[2][j] = hhval[1][j];
+      hh[0][j] += hhc[j];
       hh[1][j] = 0.5 * hh[0][j]; hh[2][j] = hh[1][j];
     }
   } else {
@@ -352,6 +475,19 @@ void o_rho2(const owfn *w, const double xpos[3], int nder, double rho[3], double
       rhoval[s] = rh[s];
       for (int j = 0; j < 3; j++) gradval[3 * s + j] = g[s][j];
       for (int j = 0; j < 6; j++) hhval[s][j] = hh[s][j];
+    }
+    rh[0] += rhoc;
+    rh[1] += 0.5 * rhoc;
+    rh[2] += 0.5 * rhoc;
+    for (int j = 0; j < 3; j++) {
+      g[0][j] += gradc[j];
+      g[1][j] += 0.5 * gradc[j];
+      g[2][j] += 0.5 * gradc[j];
+    }
+    for (int j = 0; j < 6; j++) {
+      hh[0][j] += hhc[j];
+      hh[1][j] += 0.5 * hhc[j];
+      hh[2][j] += 0.5 * hhc[j];
     }
   }
   for (int s = 0; s < 3; s++) rho[s] = rh[s];

@@ -47,6 +47,9 @@ owfn *o_wfn_new(int natom, const double *xyz, const int *z, int npri, int nmo,
                 const int *icenter, const int *itype, const double *e,
                 const double *occ, const double *cmo, int wfntyp, int nalpha);
 void o_wfn_free(owfn *w);
+/* EDF core density (1-based icenter; nedf = 0 removes it) */
+void o_wfn_set_edf(owfn *w, int nedf, const int *icenter, const int *itype, const double *e,
+                   const double *c);
 int o_wfn_npri(const owfn *w);
 void o_wfn_cell(const owfn *w, double lo[3], double aa[3], double molborder[3]);
 

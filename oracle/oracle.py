@@ -51,6 +51,7 @@ def lib():
         L.o_wfn_new.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, _ip, _ip, _dp, _dp, _dp,
                                 C.c_int, C.c_int]
         L.o_wfn_free.argtypes = [C.c_void_p]
+        L.o_wfn_set_edf.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp]
         L.o_wfn_npri.argtypes = [C.c_void_p]
         L.o_wfn_cell.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.o_rho2.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -100,6 +101,13 @@ class Wfn:
                              mol.npri, mol.nmo, _i32(mol.icenter), _i32(mol.itype), _f64(mol.e),
                              _f64(mol.occ), _f64(mol.cmo.reshape(-1)), int(mol.wfntyp),
                              int(mol.nalpha))
+        if getattr(mol, "edf_e", None) is not None and len(mol.edf_e):
+            self.set_edf(mol.edf_icenter, mol.edf_itype, mol.edf_e, mol.edf_c)
+
+    def set_edf(self, icenter, itype, e, c):
+        """EDF core density (1-based icenter and li type; empty removes it)."""
+        n = len(e)
+        lib().o_wfn_set_edf(self.h, n, _i32(icenter), _i32(itype), _f64(e), _f64(c))
 
     def __del__(self):
         if getattr(self, "h", None):

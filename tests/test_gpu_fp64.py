@@ -81,6 +81,14 @@ def test_rho2_open_shell(gpu_lib, oracle_mod, mol12, wfntyp):
         assert close(out["grad"][i], ref["grad"])
         assert close(out["hess"][i], ref["h"])
         assert close(out["gkin"][i], ref["gkin"])
+    # the density-only and first-derivative records keep the spin channels
+    for nder in (0, 1):
+        out = g.rho2(pts, nder, "fp64")
+        for i in range(0, 64, 4):
+            ref = o.rho2(pts[i], nder)
+            assert close(out["rho"][i], ref["rho"])
+            if nder:
+                assert close(out["grad"][i], ref["grad"])
 
 
 def test_grd(pair12, mol12):
