@@ -212,3 +212,29 @@ class Wavefunction:
         return dict(xyz=xyz[:n], typ=typ[:n], f=f[:n], counts=np.array(rep.count[:]),
                     ph=rep.poincare_hopf, nseed=rep.nseed, nconverged=rep.nconverged,
                     ms=rep.ms_total)
+
+
+def nci_chk_write(path: str, x0, xmat, nstep, crho, cgrad) -> None:
+    """critic2's NCI checkpoint <root>.chk_nci (c2g_nci_chk_write): grid and
+    the crho, cgrad cubes as (n1, n2, n3) arrays (k fastest in memory)."""
+    ns = _i32(nstep)
+    n = int(np.prod(ns))
+    c, g = _f64(crho).reshape(-1), _f64(cgrad).reshape(-1)
+    if c.size != n or g.size != n:
+        raise ValueError("crho and cgrad must hold nstep(1)*nstep(2)*nstep(3) values")
+    xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+    L.check(L.lib().c2g_nci_chk_write(path.encode(), _f64(x0), xm, ns, c, g))
+
+
+def nci_chk_read(path: str, x0, xmat, nstep):
+    """Loads a checkpoint that matches the grid (c2g_nci_chk_read): returns
+    (crho, cgrad) as (n1, n2, n3) arrays, or None when the file is missing
+    or belongs to another grid (critic2 then recomputes)."""
+    ns = _i32(nstep)
+    shape = tuple(int(v) for v in ns)
+    crho, cgrad = np.zeros(shape), np.zeros(shape)
+    found = C.c_int(0)
+    xm = _f64(np.asarray(xmat, np.float64).T.reshape(-1))
+    L.check(L.lib().c2g_nci_chk_read(path.encode(), _f64(x0), xm, ns, crho.reshape(-1), cgrad.reshape(-1),
+                                     C.byref(found)))
+    return (crho, cgrad) if found.value else None

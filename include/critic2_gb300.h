@@ -245,6 +245,20 @@ int c2g_dat_text(const double *d_dat, long ndat, char *text, long cap, long *nby
 int c2g_nciplot_files(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec,
                       const char *root, const c2g_nci_cut *cut, c2g_nci_stats *stats, double *ms_parts);
 
+/* nciplot's checkpoint file <root>.chk_nci (writechk / readchk,
+ * src/nci@proc.f90:1019-1117), byte-compatible with critic2's (gfortran
+ * unformatted sequential records): the grid (x0(3), xmat(3,3) columns,
+ * nstep(3)) and the host cubes crho, cgrad in (k,j,i) order, without
+ * promolecular or fragment densities.  c2g_nci_chk_read loads the cubes
+ * when the file exists and matches x0 and xmat to 1e-13 and nstep exactly
+ * (*found = 1); a missing or non-matching file gives *found = 0 and
+ * C2G_OK, as readchk restarts the calculation; a truncated or malformed
+ * file gives C2G_ERR_IO (crho and cgrad are then undefined). */
+int c2g_nci_chk_write(const char *path, const double *x0, const double *xmat, const int *nstep,
+                      const double *crho, const double *cgrad);
+int c2g_nci_chk_read(const char *path, const double *x0, const double *xmat, const int *nstep, double *crho,
+                     double *cgrad, int *found);
+
 /* Quantities of field%grd for CUBE plots (rhoplot_cube's nti selectors,
  * src/rhoplot@proc.f90:905-930). */
 #define C2G_FIELD_RHO 0

@@ -270,3 +270,84 @@ def precise_body(nstep, values) -> str:
             chunk = row[c:c + 6]
             out.append("".join(" " + fmt_E22(x) for x in chunk) + (" " if len(chunk) < 6 else "") + "\n")
     return "".join(out)
+
+
+# ------------------------------------------------------------ NCI checkpoint
+# gfortran's unformatted sequential layout (libgfortran, the runtime of the
+# reference's usual compiler; its record format is documented in the GNU
+# Fortran manual, "Unformatted sequential file format"): each record is
+# one or more subrecords, each framed by 4-byte length markers; the leading
+# marker of every subrecord but the last is negative, the trailing marker
+# of every subrecord but the first is negative; at most 2^31 - 9 data bytes
+# per subrecord.
+MAX_SUBRECORD = 2147483639
+
+
+def fortran_records_bytes(records, maxsub=MAX_SUBRECORD) -> bytes:
+    """The bytes of a sequence of records (each a bytes object)."""
+    out = []
+    for rec in records:
+        n = len(rec)
+        pos, first = 0, True
+        while True:
+            m = min(n - pos, maxsub)
+            last = pos + m == n
+            out.append(np.int32(m if last else -m).tobytes())
+            out.append(rec[pos:pos + m])
+            out.append(np.int32(m if first else -m).tobytes())
+            pos += m
+            first = False
+            if last:
+                break
+    return b"".join(out)
+
+
+def fortran_records_parse(data: bytes):
+    """Splits gfortran unformatted sequential bytes into records."""
+    recs, pos = [], 0
+    while pos < len(data):
+        parts, more = [], True
+        while more:
+            lead = int(np.frombuffer(data[pos:pos + 4], np.int32)[0])
+            m = abs(lead)
+            parts.append(data[pos + 4:pos + 4 + m])
+            trail = int(np.frombuffer(data[pos + 4 + m:pos + 8 + m], np.int32)[0])
+            assert abs(trail) == m, "bad record marker"
+            pos += 8 + m
+            more = lead < 0
+        recs.append(b"".join(parts))
+    return recs
+
+
+def nci_chk_records(x0, xmat, nstep, crho, cgrad, rhoat=None, nfrag=0):
+    """writechk's records (src/nci@proc.f90:1087-1117); xmat[:, i] is step i;
+    logicals as gfortran's default LOGICAL (4 bytes, 1 = .true.)."""
+    xm = np.asarray(xmat, np.float64)
+    recs = [np.array([int(rhoat is not None), 0, nfrag], np.int32).tobytes(),
+            _f64(x0).tobytes()] + [_f64(xm[:, j]).tobytes() for j in range(3)]
+    recs.append(_i32(nstep).tobytes())
+    recs.append(_f64(crho).reshape(-1).tobytes() + _f64(cgrad).reshape(-1).tobytes())
+    if rhoat is not None:
+        recs.append(_f64(rhoat).reshape(-1).tobytes())
+    return recs
+
+
+def nci_chk_read(data: bytes, x0, xmat, nstep):
+    """readchk (src/nci@proc.f90:1019-1085) for a caller without promolecular
+    or fragment densities: (crho, cgrad) flat arrays, or None when the file
+    does not match the grid."""
+    r = fortran_records_parse(data)
+    llat, llfrag, nfrag0 = np.frombuffer(r[0][:12], np.int32)
+    if nfrag0 != 0:
+        return None
+    xm = np.asarray(xmat, np.float64)
+    if np.any(np.abs(np.frombuffer(r[1][:24]) - _f64(x0)) > 1e-13):
+        return None
+    for j in range(3):
+        if np.any(np.abs(np.frombuffer(r[2 + j][:24]) - xm[:, j]) > 1e-13):
+            return None
+    if np.any(np.frombuffer(r[5][:12], np.int32) != _i32(nstep)):
+        return None
+    n = int(np.prod(nstep))
+    v = np.frombuffer(r[6][:16 * n])
+    return v[:n].copy(), v[n:].copy()
