@@ -200,6 +200,23 @@ class Wavefunction:
         L.check(L.lib().c2g_pair_seeds(self._h, maxdist, npts, L.ptr(buf), C.byref(n)))
         return buf[: n.value]
 
+    def cp_graph(self, cp_xyz, cp_typ) -> dict:
+        """makegraph over a CP list (c2g_cp_graph): ipath (n,2) 1-based
+        terminator indices (0 none, -1 outside), brdist (n,2), brpathlen
+        (n,2), brang (n,), brvec (n,3), ier (n,2), nstep (n,2), stats."""
+        x = _f64(cp_xyz).reshape(-1, 3)
+        t = _i32(cp_typ)
+        n = t.shape[0]
+        o = dict(ipath=np.zeros((n, 2), np.int32), brdist=np.zeros((n, 2)), brpathlen=np.zeros((n, 2)),
+                 brang=np.zeros(n), brvec=np.zeros((n, 3)), ier=np.zeros((n, 2), np.int32),
+                 nstep=np.zeros((n, 2), np.int32))
+        st = L.GraphStats()
+        L.check(L.lib().c2g_cp_graph(self._h, n, L.ptr(x), L.ptr(t), L.ptr(o["ipath"]), L.ptr(o["brdist"]),
+                                     L.ptr(o["brpathlen"]), L.ptr(o["brang"]), L.ptr(o["brvec"]),
+                                     L.ptr(o["ier"]), L.ptr(o["nstep"]), C.byref(st)))
+        o["stats"] = dict(npath=st.npath, nbatch=st.nbatch, nevals=st.nevals, ms=st.ms_total)
+        return o
+
     def autocritic(self, seeds: Optional[np.ndarray] = None, prec="fp64") -> dict:
         s = None if seeds is None else _f64(seeds).reshape(-1, 3)
         ns = 0 if s is None else s.shape[0]

@@ -324,6 +324,40 @@ typedef struct {
 int c2g_autocritic(c2g_wfn *h, int nseed, const double *xseed, int prec, int maxcp,
                    double *cp_xyz, int *cp_typ, double *cp_f, c2g_cp_report *report);
 
+/* The molecular graph that autocritic builds after the CP search
+ * (makegraph, src/autocp@proc.f90:2116-2268; autocritic runs it by
+ * default, dograph = 1).  From every bond CP (typ -1) two gradient paths go
+ * up the density from r +- 0.01 e, e the Hessian eigenvector of the
+ * positive curvature; from every ring CP (typ +1) two go down along the
+ * negative one.  Paths follow field%gradient (src/fieldmod@proc.f90:
+ * 2500-2732) with critic2's default navigation: Bogacki-Shampine stepper,
+ * step 0.3 bohr, maxerr 1e-4, gradeps 1e-7, beta spheres 0.1 bohr; they end
+ * in the beta sphere of the nearest nucleus or CP of type 3 typ, at a new
+ * CP, on leaving the molecular cell (down paths), on bouncing, or after
+ * 3333 steps.  The CP list is c2g_autocritic's (nuclei included, typ -3).
+ * Outputs, column-major (j = 1, 2 are the two paths):
+ *   ipath(2,ncp)     1-based CP index of type 3 typ nearest to the end
+ *                    point (no distance limit); -1 when there is none and
+ *                    the end point is outside the molecular cell's inner
+ *                    region; 0 otherwise, and for CPs with |typ| /= 1
+ *   brdist(2,ncp)    |end point - CP|;  brpathlen(2,ncp) path length
+ *   brang(ncp)       angle (degrees) between the two end vectors
+ *   brvec(3,ncp)     the unit eigenvector e
+ *   ier(2,ncp), nstep(2,ncp)   field%gradient's ier and step count (may be NULL)
+ * The paths are traced together, one GPU batch of FP64 evaluations per
+ * Runge-Kutta stage.  The sign of e follows a fixed rule (largest
+ * component positive), not LAPACK's, so the two paths of a CP may be
+ * listed in the other order than critic2 lists them. */
+typedef struct {
+  int npath;       /* gradient paths traced */
+  int nbatch;      /* GPU evaluation batches */
+  long nevals;     /* field evaluations */
+  double ms_total; /* wall time of the call */
+} c2g_graph_stats;
+
+int c2g_cp_graph(c2g_wfn *h, int ncp, const double *cp_xyz, const int *cp_typ, int *ipath, double *brdist,
+                 double *brpathlen, double *brang, double *brvec, int *ier, int *nstep, c2g_graph_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -861,6 +861,270 @@ int o_autocritic(const owfn *w, int nseed, const double *xseed, int nthreads, in
   return ncp;
 }
 
+/* ------------------------------------------------------- molecular graph */
+/* Symmetric 3x3 eigenvalues and eigenvectors (column-major input), the role
+ * of eigsym (LAPACK dsyev 'V', src/tools_math@proc.f90:1005-1039): cyclic
+ * Jacobi, eigenvalues ascending, vec column j (vec[3*j..3*j+2]) for ev[j].
+ * dsyev's sign of an eigenvector is not reproduced: each vector is scaled
+ * so that its component of largest magnitude (the first such) is positive. */
+void o_eigvec3(const double m[9], double ev[3], double vec[9]) {
+  double a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) a[i][j] = 0.5 * (m[3 * j + i] + m[3 * i + j]);
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    double dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off == 0.0 || off < 1e-34 * dia) break;
+    for (int p = 0; p < 2; p++)
+      for (int q = p + 1; q < 3; q++) {
+        if (a[p][q] == 0.0) continue;
+        double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; k++) {
+          double akp = a[k][p], akq = a[k][q];
+          a[k][p] = c * akp - s * akq;
+          a[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; k++) {
+          double apk = a[p][k], aqk = a[q][k];
+          a[p][k] = c * apk - s * aqk;
+          a[q][k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; k++) {
+          double vkp = v[k][p], vkq = v[k][q];
+          v[k][p] = c * vkp - s * vkq;
+          v[k][q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  int ord[3] = {0, 1, 2};
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2 - i; j++)
+      if (a[ord[j]][ord[j]] > a[ord[j + 1]][ord[j + 1]]) { int t = ord[j]; ord[j] = ord[j + 1]; ord[j + 1] = t; }
+  for (int j = 0; j < 3; j++) {
+    int c = ord[j];
+    ev[j] = a[c][c];
+    int big = 0;
+    for (int k = 1; k < 3; k++)
+      if (fabs(v[k][c]) > fabs(v[big][c])) big = k;
+    double sg = v[big][c] < 0.0 ? -1.0 : 1.0;
+    for (int k = 0; k < 3; k++) vec[3 * j + k] = sg * v[k][c];
+  }
+}
+
+#define NAV_STEP 0.3      /* src/global@proc.F90:859 */
+#define NAV_MAXERR 1e-4   /* :860 */
+#define NAV_GRADEPS 1e-7  /* :861 */
+#define RBETADEF 0.1      /* src/global.f90:41 */
+
+static void unit_grad(const ores *r, double g[3]) {
+  for (int j = 0; j < 3; j++) g[j] = r->gf[j] / (r->gfmod + VSMALL);
+}
+
+/* stepper_bs, src/fieldmod@proc.f90:2860-2890 (Bogacki-Shampine 2(3),
+ * FSAL): res ends as the evaluation at xout. */
+static void stepper_bs(const owfn *w, const double x[3], const double ak1[3], double h0, double xout[3],
+                       double xerr[3], ores *res) {
+  double ak2[3], ak3[3], ak4[3], xt[3];
+  for (int j = 0; j < 3; j++) xt[j] = x[j] + h0 * (0.5 * ak1[j]);
+  o_grd(w, xt, 2, res);
+  unit_grad(res, ak2);
+  for (int j = 0; j < 3; j++) xt[j] = x[j] + h0 * (0.75 * ak2[j]);
+  o_grd(w, xt, 2, res);
+  unit_grad(res, ak3);
+  for (int j = 0; j < 3; j++) xout[j] = x[j] + h0 * (2.0 / 9.0 * ak1[j] + 1.0 / 3.0 * ak2[j] + 4.0 / 9.0 * ak3[j]);
+  o_grd(w, xout, 2, res);
+  unit_grad(res, ak4);
+  for (int j = 0; j < 3; j++)
+    xerr[j] = x[j] + h0 * (7.0 / 24.0 * ak1[j] + 1.0 / 4.0 * ak2[j] + 1.0 / 3.0 * ak3[j] + 1.0 / 8.0 * ak4[j]) -
+              xout[j];
+}
+
+/* adaptive_stepper with the BS stepper, src/fieldmod@proc.f90:2737-2830.
+ * As in the reference, a rejected trial leaves its end-point gradient as
+ * the first stage of the next trial. */
+static int adaptive_stepper(const owfn *w, double x[3], double *h0, double maxstep, ores *res) {
+  double grdt[3], xtemp[3], xerr[3];
+  unit_grad(res, grdt);
+  int first = 1;
+  for (;;) {
+    stepper_bs(w, x, grdt, *h0, xtemp, xerr, res);
+    unit_grad(res, grdt);
+    double nerr = sqrt(xerr[0] * xerr[0] + xerr[1] * xerr[1] + xerr[2] * xerr[2]);
+    if (nerr < NAV_MAXERR) {
+      for (int j = 0; j < 3; j++) x[j] = xtemp[j];
+      if (first && nerr < NAV_MAXERR / 10.0)
+        *h0 = copysign(fmin(fabs(maxstep), fabs(1.6 * *h0)), maxstep);
+      return 1;
+    }
+    *h0 = 0.9 * *h0 * NAV_MAXERR / nerr;
+    if (fabs(*h0) < VSMALL) return 0;
+    first = 0;
+  }
+}
+
+/* field%gradient for a molecule, src/fieldmod@proc.f90:2500-2732, with
+ * critic2's default navigation (BS stepper, step 0.3, maxerr 1e-4,
+ * gradeps 1e-7) and up2beta: a path stops in the beta sphere (0.1 bohr) of
+ * the nearest CP of the attracting kind (-3 up, +3 down; the nearest
+ * non-hydrogen nucleus counts first when going up), at a new CP
+ * (|grad| < gradeps), when it leaves the molecular cell's inner region
+ * (going down, ier 3), when it bounces (5 reversals) or the step falls
+ * under 1e-12 (ier 1), or after nint(1000/0.3) steps (ier 2).  x: start
+ * (in) and end point (out); plen starts at |x - pathini|. */
+int o_gradient(const owfn *w, double x[3], int iup, int ncp, const double *cpx, const int *cptyp,
+               const double pathini[3], int *nstep_out, double *plen_out) {
+  const double minstep = 1e-12, hfirst = 0.01;
+  const int mhist = 5;
+  double hini = NAV_STEP * iup, h0 = hfirst * iup;
+  double scalhist[5] = {1, 1, 1, 1, 1};
+  int nhist = 0, ier = 0, incstep = 0, nstep;
+  double xlast[3], xlast2[3];
+  for (int j = 0; j < 3; j++) xlast[j] = xlast2[j] = x[j];
+  double plen = sqrt((x[0] - pathini[0]) * (x[0] - pathini[0]) + (x[1] - pathini[1]) * (x[1] - pathini[1]) +
+                     (x[2] - pathini[2]) * (x[2] - pathini[2]));
+  const int mstep = (int)lround(10000 * 0.1 / fabs(hini));
+  ores res;
+  o_grd(w, x, 2, &res);
+  for (nstep = 1; nstep <= mstep; nstep++) {
+    double d[3];
+    for (int j = 0; j < 3; j++) d[j] = x[j] - xlast[j];
+    plen += sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    /* nearest nucleus, then nearer CPs of the attracting kind */
+    double sphrad;
+    int idnuc = identify_atom(w, x, 1e300, &sphrad);
+    int idcp = -1;
+    double cprad = 1e15, xcp[3] = {0, 0, 0};
+    if (iup == 1 && w->z[idnuc] != 1) {
+      idcp = idnuc;
+      cprad = sphrad;
+      for (int j = 0; j < 3; j++) xcp[j] = w->xyz[3 * idnuc + j];
+    }
+    for (int i = 0; i < ncp; i++) {
+      if (!((cptyp[i] == -3 && iup == 1) || (cptyp[i] == 3 && iup == -1))) continue;
+      double dx = x[0] - cpx[3 * i], dy = x[1] - cpx[3 * i + 1], dz = x[2] - cpx[3 * i + 2];
+      double dist = sqrt(dx * dx + dy * dy + dz * dz);
+      if (dist < cprad) {
+        cprad = dist;
+        idcp = i;
+        for (int j = 0; j < 3; j++) xcp[j] = cpx[3 * i + j];
+      }
+    }
+    if (idcp >= 0 && cprad <= RBETADEF) {
+      incstep = 1;
+      double e2 = 0.0;
+      for (int j = 0; j < 3; j++) e2 += (x[j] - xcp[j]) * (x[j] - xcp[j]);
+      plen += sqrt(e2);
+      for (int j = 0; j < 3; j++) x[j] = xcp[j];
+      ier = 0;
+      goto done;
+    }
+    if (iup == -1) {
+      for (int j = 0; j < 3; j++) {
+        double xf = (x[j] - w->cell_lo[j]) / w->aa[j];
+        if (xf < w->molborder[j] || xf > 1.0 - w->molborder[j]) { ier = 3; goto done; }
+      }
+    }
+    if (res.gfmod < NAV_GRADEPS) { ier = 0; goto done; }
+    for (int j = 0; j < 3; j++) xlast2[j] = xlast[j], xlast[j] = x[j];
+    int ok = adaptive_stepper(w, x, &h0, hini, &res);
+    nhist = nhist % mhist + 1;
+    double sc = 0.0;
+    for (int j = 0; j < 3; j++) sc += (xlast[j] - xlast2[j]) * (x[j] - xlast[j]);
+    scalhist[nhist - 1] = sc;
+    int allneg = 1;
+    for (int k = 0; k < mhist; k++) allneg &= scalhist[k] < 0.0;
+    ok = ok && !allneg;
+    if (!ok || fabs(h0) < minstep) {
+      for (int j = 0; j < 3; j++) x[j] = xlast[j];
+      ier = 1;
+      goto done;
+    }
+  }
+  nstep = mstep;
+  ier = 2;
+done:
+  if (incstep) nstep++;
+  *nstep_out = nstep;
+  *plen_out = plen;
+  return ier;
+}
+
+/* makegraph, src/autocp@proc.f90:2116-2268, for a molecule without
+ * symmetry: for each bond (typ -1) and ring (typ +1) CP, two paths from
+ * r +- 0.01 e (e: Hessian eigenvector of the largest eigenvalue for a bond
+ * CP, of the smallest for a ring CP), up for bonds and down for rings;
+ * ipath(j) = 1-based index of the CP of type 3 typ nearest to the end
+ * point (no distance limit), -1 when there is none and the end point is
+ * outside the molecular cell's inner region, else 0; brdist = |end - r|,
+ * brpathlen = path length, brang = angle (degrees) between the two end
+ * vectors.  Other CPs get zeros.  Arrays: ipath, brdist, brpathlen, ier,
+ * nstep (2, ncp); brang (ncp); brvec (3, ncp). */
+void o_makegraph(const owfn *w, int ncp, const double *cpx, const int *cptyp, int *ipath, double *brdist,
+                 double *brpathlen, double *brang, double *brvec, int *ier, int *nstep, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic)
+  for (int i = 0; i < ncp; i++) {
+    for (int j = 0; j < 2; j++) {
+      ipath[2 * i + j] = 0, brdist[2 * i + j] = 0.0, brpathlen[2 * i + j] = 0.0;
+      ier[2 * i + j] = 0, nstep[2 * i + j] = 0;
+    }
+    brang[i] = 0.0;
+    for (int k = 0; k < 3; k++) brvec[3 * i + k] = 0.0;
+    if (abs(cptyp[i]) != 1) continue;
+    const int isbcp = cptyp[i] == -1;
+    const double *r = cpx + 3 * i;
+    ores res;
+    o_grd(w, r, 2, &res);
+    double ev[3], vec[9], xx[3];
+    o_eigvec3(res.hf, ev, vec);
+    const double *e = isbcp ? vec + 6 : vec;
+    double nn = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    for (int k = 0; k < 3; k++) xx[k] = e[k] / nn;
+    double xd[2][3], xdif[2][3];
+    for (int j = 0; j < 2; j++) {
+      for (int k = 0; k < 3; k++) xd[j][k] = r[k] + (j == 0 ? 1.0 : -1.0) * 0.01 * xx[k];
+      ier[2 * i + j] = o_gradient(w, xd[j], isbcp ? 1 : -1, ncp, cpx, cptyp, r, &nstep[2 * i + j],
+                                  &brpathlen[2 * i + j]);
+    }
+    for (int k = 0; k < 3; k++) brvec[3 * i + k] = xx[k];
+    for (int j = 0; j < 2; j++) {
+      double dd = 0.0;
+      for (int k = 0; k < 3; k++) xdif[j][k] = xd[j][k] - r[k], dd += xdif[j][k] * xdif[j][k];
+      brdist[2 * i + j] = sqrt(dd);
+      /* nearest CP of type 3*typ, end point wrapped into the cell */
+      double xf[3], best = 1e30;
+      int wcp = 0, outside = 0;
+      for (int k = 0; k < 3; k++) {
+        double f = (xd[j][k] - w->cell_lo[k]) / w->aa[k];
+        if (f < w->molborder[k] || f > 1.0 - w->molborder[k]) outside = 1;
+        xf[k] = f - floor(f);
+      }
+      for (int c = 0; c < ncp; c++) {
+        if (cptyp[c] != 3 * cptyp[i]) continue;
+        double d2 = 0.0;
+        for (int k = 0; k < 3; k++) {
+          double t = ((cpx[3 * c + k] - w->cell_lo[k]) / w->aa[k] - xf[k]) * w->aa[k];
+          d2 += t * t;
+        }
+        double dist = sqrt(d2);
+        if (dist < best) best = dist, wcp = c + 1;
+      }
+      ipath[2 * i + j] = wcp ? wcp : (outside ? -1 : 0);
+    }
+    double ca = 0.0;
+    if (brdist[2 * i] > 1e-12) {
+      for (int k = 0; k < 3; k++) ca += xdif[0][k] * xdif[1][k];
+      ca = ca / brdist[2 * i] / brdist[2 * i + 1];
+    }
+    if (fabs(ca) > 1.0) ca = ca / fabs(ca);
+    brang[i] = acos(ca) * 180.0 / M_PI;
+  }
+}
+
 /* ------------------------------------------------------------ NCI output */
 /* Fortran list output of (" ",1p,e13.5e3): blank, then the number right-
  * justified in 13 columns with 6 significant digits and a 3-digit

@@ -92,6 +92,14 @@ long o_cube_body(const int nstep[3], const double *v, char *out);
 long o_nci_post(const int nstep[3], const double *crho, double *cgrad, double rhocut, double dimcut,
                 double rhoplot, double srho_lo, double srho_hi, int onlyneg, double *dat);
 
+/* Molecular graph: Hessian eigenvectors, field%gradient, makegraph
+ * (src/fieldmod@proc.f90:2500-2890, src/autocp@proc.f90:2116-2268). */
+void o_eigvec3(const double m[9], double ev[3], double vec[9]);
+int o_gradient(const owfn *w, double x[3], int iup, int ncp, const double *cpx, const int *cptyp,
+               const double pathini[3], int *nstep, double *plen);
+void o_makegraph(const owfn *w, int ncp, const double *cpx, const int *cptyp, int *ipath, double *brdist,
+                 double *brpathlen, double *brang, double *brvec, int *ier, int *nstep, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,11 @@ def lib():
         L.o_pair_seeds.restype = C.c_int
         L.o_autocritic.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, C.c_int, _dp, _ip, _dp, _ip]
         L.o_autocritic.restype = C.c_int
+        L.o_eigvec3.argtypes = [_dp, _dp, _dp]
+        L.o_gradient.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, _dp, _ip, _dp, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]
+        L.o_gradient.restype = C.c_int
+        L.o_makegraph.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, C.c_int]
         L.o_fmt_e13_5e3.argtypes = [C.c_double, C.c_char_p]
         L.o_fmt_E15_7.argtypes = [C.c_double, C.c_char_p]
         L.o_fmt_E22_14E3.argtypes = [C.c_double, C.c_char_p]
@@ -177,6 +182,28 @@ class Wfn:
         lib().o_pair_seeds(self.h, maxdist, npts, buf, n)
         return buf[: 3 * n].reshape(n, 3)
 
+    def gradient(self, x, iup, cp_xyz, cp_typ, pathini):
+        """field%gradient (molecule, default navigation, up2beta): returns
+        (end point, ier, nstep, plen)."""
+        xx = _f64(x).copy()
+        ns, pl = C.c_int(0), C.c_double(0.0)
+        cx, ct = _f64(cp_xyz).reshape(-1), _i32(cp_typ)
+        ier = lib().o_gradient(self.h, xx, int(iup), len(ct), cx, ct, _f64(pathini), C.byref(ns), C.byref(pl))
+        return xx, ier, ns.value, pl.value
+
+    def makegraph(self, cp_xyz, cp_typ, nthreads=0):
+        """makegraph over a CP list: dict of ipath (n,2), brdist (n,2),
+        brpathlen (n,2), brang (n,), brvec (n,3), ier (n,2), nstep (n,2)."""
+        ct = _i32(cp_typ)
+        n = len(ct)
+        out = dict(ipath=np.zeros((n, 2), np.int32), brdist=np.zeros((n, 2)), brpathlen=np.zeros((n, 2)),
+                   brang=np.zeros(n), brvec=np.zeros((n, 3)), ier=np.zeros((n, 2), np.int32),
+                   nstep=np.zeros((n, 2), np.int32))
+        lib().o_makegraph(self.h, n, _f64(cp_xyz).reshape(-1), ct, out["ipath"].reshape(-1),
+                          out["brdist"].reshape(-1), out["brpathlen"].reshape(-1), out["brang"],
+                          out["brvec"].reshape(-1), out["ier"].reshape(-1), out["nstep"].reshape(-1), nthreads)
+        return out
+
     def autocritic(self, seeds=None, nthreads=0):
         if seeds is None:
             seeds = self.pair_seeds()
@@ -188,6 +215,13 @@ class Wfn:
                                  xyz, typ, f, cnt)
         return dict(xyz=xyz[: 3 * ncp].reshape(ncp, 3), typ=typ[:ncp], f=f[:ncp],
                     counts=cnt, ph=int(cnt[0] - cnt[1] + cnt[2] - cnt[3]))
+
+
+def eigvec3(m):
+    """Ascending eigenvalues and eigenvectors (columns) of a 3x3 matrix."""
+    ev, v = np.zeros(3), np.zeros(9)
+    lib().o_eigvec3(_f64(np.asarray(m).reshape(-1)), ev, v)
+    return ev, v.reshape(3, 3).T
 
 
 def eigsym3(m):
