@@ -171,8 +171,13 @@ def run_reference(args, wl, mol):
         o = oracle.Wfn(cmol)
         t0 = time.perf_counter()
         r = o.autocritic(nthreads=threads)
+        ms_plain = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        o.makegraph(r["xyz"], r["typ"], nthreads=threads)
+        ms_graph = 1e3 * (time.perf_counter() - t0)
         line["cp_search"] = {"workload": f"cp100: {cmol.natom} atoms, {cmol.npri} primitives, {cmol.nmo} MOs",
-                             "unit": "ms", "ms_plain": 1e3 * (time.perf_counter() - t0),
+                             "unit": "ms", "ms_plain": ms_plain, "ms_graph": ms_graph,
+                             "graph_paths": int(2 * (abs(r["typ"]) == 1).sum()),
                              "ncp": int(len(r["xyz"])), "ph": int(r["ph"]), "cores": threads,
                              "kind": "port"}
     print(json.dumps(line), flush=True)
@@ -197,6 +202,17 @@ def cp_search(args):
         out[f"{prec}, newton_stall {stall}"] = {k: st[k] for k in ("ms_plain", "ms_learned", "speedup", "recall", "recall_outside_cores",
                                         "ncp", "ncp_outside_cores", "plain_ph", "learned_ph", "stage", "reason",
                                         "plain_seeds", "learned_seeds", "proposal", "grid_seeds")}
+    # AUTO's graph stage (makegraph: two gradient paths per bond and ring
+    # CP) on the FP64 pair-seed CP list, through c2g_cp_graph
+    from critic2_gb300.wfn import Wavefunction
+    w = Wavefunction(mol)
+    cp = w.autocritic(prec="fp64")
+    w.cp_graph(cp["xyz"], cp["typ"])  # warm-up
+    t0 = time.perf_counter()
+    g = w.cp_graph(cp["xyz"], cp["typ"])
+    out["graph"] = {"ms": 1e3 * (time.perf_counter() - t0), "cps": int(len(cp["typ"])),
+                    "paths": g["stats"]["npath"], "batches": g["stats"]["nbatch"],
+                    "evaluations": g["stats"]["nevals"]}
     return out
 
 

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <vector>
 
@@ -85,33 +86,54 @@ void eigvec3(const double m[9], double ev[3], double vec[9]) {
 // a nucleus, on the wrapped position) on the host.
 class BatchGrd {
  public:
+  // One staging buffer each way in pinned memory and one stream: a batch is
+  // one upload (count + points), the kernel, one download and one sync.
   BatchGrd(Handle &h, int cap) : h_(h), cap_(std::max(cap, 1)) {
-    C2G_CUDA(cudaMalloc(&d_x_, sizeof(double) * 3 * cap_));
-    C2G_CUDA(cudaMalloc(&d_idx_, sizeof(int) * cap_));
-    C2G_CUDA(cudaMalloc(&d_cnt_, sizeof(int)));
-    C2G_CUDA(cudaMalloc(&d_rec_, sizeof(double) * kRecNci * cap_));
-    std::vector<int> iota(cap_);
-    std::iota(iota.begin(), iota.end(), 0);
-    C2G_CUDA(cudaMemcpy(d_idx_, iota.data(), sizeof(int) * cap_, cudaMemcpyHostToDevice));
-    rec_.resize((size_t)kRecNci * cap_);
+    try {
+      allocate();
+    } catch (...) {
+      release();
+      throw;
+    }
   }
-  ~BatchGrd() {
-    cudaFree(d_x_);
-    cudaFree(d_idx_);
-    cudaFree(d_cnt_);
-    cudaFree(d_rec_);
-  }
+  ~BatchGrd() { release(); }
   BatchGrd(const BatchGrd &) = delete;
   BatchGrd &operator=(const BatchGrd &) = delete;
 
+ private:
+  void allocate() {
+    C2G_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    C2G_CUDA(cudaMalloc(&d_in_, sizeof(double) * (1 + 3 * (size_t)cap_)));
+    C2G_CUDA(cudaMalloc(&d_idx_, sizeof(int) * cap_));
+    C2G_CUDA(cudaMalloc(&d_rec_, sizeof(double) * kRecNci * cap_));
+    C2G_CUDA(cudaMallocHost(&h_in_, sizeof(double) * (1 + 3 * (size_t)cap_)));
+    C2G_CUDA(cudaMallocHost(&h_rec_, sizeof(double) * kRecNci * cap_));
+    std::vector<int> iota(cap_);
+    std::iota(iota.begin(), iota.end(), 0);
+    C2G_CUDA(cudaMemcpy(d_idx_, iota.data(), sizeof(int) * cap_, cudaMemcpyHostToDevice));
+  }
+  void release() {
+    if (st_) cudaStreamSynchronize(st_);
+    if (d_in_) cudaFree(d_in_);
+    if (d_idx_) cudaFree(d_idx_);
+    if (d_rec_) cudaFree(d_rec_);
+    if (h_in_) cudaFreeHost(h_in_);
+    if (h_rec_) cudaFreeHost(h_rec_);
+    if (st_) cudaStreamDestroy(st_);
+    st_ = nullptr, d_in_ = d_rec_ = h_in_ = h_rec_ = nullptr, d_idx_ = nullptr;
+  }
+
+ public:
   // xyz(3, n) -> rec(10, n) with the nucleus rule applied to the gradient
   const double *eval(const double *xyz, int n) {
-    if (n <= 0) return rec_.data();
+    if (n <= 0) return h_rec_;
     if (n > cap_) fail(C2G_ERR_ARG, "gradient-path batch larger than its buffers");
-    C2G_CUDA(cudaMemcpy(d_x_, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
-    C2G_CUDA(cudaMemcpy(d_cnt_, &n, sizeof(int), cudaMemcpyHostToDevice));
-    launch_fp64_index(h_.dev, d_x_, d_idx_, d_cnt_, n, d_rec_, 0);
-    C2G_CUDA(cudaMemcpy(rec_.data(), d_rec_, sizeof(double) * kRecNci * n, cudaMemcpyDeviceToHost));
+    std::memcpy(h_in_, &n, sizeof(int));
+    std::memcpy(h_in_ + 1, xyz, sizeof(double) * 3 * n);
+    C2G_CUDA(cudaMemcpyAsync(d_in_, h_in_, sizeof(double) * (1 + 3 * (size_t)n), cudaMemcpyHostToDevice, st_));
+    launch_fp64_index(h_.dev, d_in_ + 1, d_idx_, reinterpret_cast<const int *>(d_in_), n, d_rec_, st_);
+    C2G_CUDA(cudaMemcpyAsync(h_rec_, d_rec_, sizeof(double) * kRecNci * n, cudaMemcpyDeviceToHost, st_));
+    C2G_CUDA(cudaStreamSynchronize(st_));
     evals_ += n;
     launches_++;
     const HostWfn &w = h_.host;
@@ -125,13 +147,13 @@ class BatchGrd {
       for (int a = 0; a < w.natom; a++) {
         const double dx = x[0] - w.xyz[3 * a], dy = x[1] - w.xyz[3 * a + 1], dz = x[2] - w.xyz[3 * a + 2];
         if (std::sqrt(dx * dx + dy * dy + dz * dz) <= 1e-5) {
-          double *q = rec_.data() + (size_t)i * kRecNci;
+          double *q = h_rec_ + (size_t)i * kRecNci;
           q[1] = q[2] = q[3] = 0.0;
           break;
         }
       }
     }
-    return rec_.data();
+    return h_rec_;
   }
   long evals() const { return evals_; }
   long launches() const { return launches_; }
@@ -139,9 +161,9 @@ class BatchGrd {
  private:
   Handle &h_;
   int cap_;
-  double *d_x_ = nullptr, *d_rec_ = nullptr;
-  int *d_idx_ = nullptr, *d_cnt_ = nullptr;
-  std::vector<double> rec_;
+  cudaStream_t st_ = nullptr;
+  double *d_in_ = nullptr, *d_rec_ = nullptr, *h_in_ = nullptr, *h_rec_ = nullptr;
+  int *d_idx_ = nullptr;
   long evals_ = 0, launches_ = 0;
 };
 
