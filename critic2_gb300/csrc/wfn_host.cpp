@@ -285,4 +285,218 @@ bool read_wfx(const char *path, HostWfn &w, std::string &err) {
   return true;
 }
 
+// ------------------------------------------------------------------ wfn
+namespace {
+
+// Element symbols by atomic number (index 0 unused).
+const char *const kElem[] = {
+    "",   "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",  "Ne", "Na", "Mg", "Al", "Si", "P",  "S",
+    "Cl", "Ar", "K",  "Ca", "Sc", "Ti", "V",  "Cr", "Mn", "Fe", "Co", "Ni", "Cu", "Zn", "Ga", "Ge", "As",
+    "Se", "Br", "Kr", "Rb", "Sr", "Y",  "Zr", "Nb", "Mo", "Tc", "Ru", "Rh", "Pd", "Ag", "Cd", "In", "Sn",
+    "Sb", "Te", "I",  "Xe", "Cs", "Ba", "La", "Ce", "Pr", "Nd", "Pm", "Sm", "Eu", "Gd", "Tb", "Dy", "Ho",
+    "Er", "Tm", "Yb", "Lu", "Hf", "Ta", "W",  "Re", "Os", "Ir", "Pt", "Au", "Hg", "Tl", "Pb", "Bi", "Po",
+    "At", "Rn", "Fr", "Ra", "Ac", "Th", "Pa", "U",  "Np", "Pu", "Am", "Cm", "Bk", "Cf", "Es", "Fm", "Md",
+    "No", "Lr", "Rf", "Db", "Sg", "Bh", "Hs", "Mt", "Ds", "Rg", "Cn", "Nh", "Fl", "Mc", "Lv", "Ts", "Og"};
+
+// Atomic number from a label such as "C", "Cl", "c12", "CL" (the role of
+// zatguess, src/tools_io@proc.f90): the letters at the start, a two-letter
+// symbol first, then one letter; 0 when nothing matches.
+int zatguess(const std::string &label) {
+  std::string l;
+  for (char c : label) {
+    if (std::isalpha((unsigned char)c)) l += c;
+    else if (!l.empty()) break;
+  }
+  if (l.empty()) return 0;
+  auto match = [&](const std::string &sym) {
+    for (int z = 1; z < (int)(sizeof(kElem) / sizeof(kElem[0])); z++) {
+      const char *e = kElem[z];
+      if (std::strlen(e) != sym.size()) continue;
+      bool ok = true;
+      for (size_t i = 0; i < sym.size(); i++)
+        ok = ok && std::tolower((unsigned char)e[i]) == std::tolower((unsigned char)sym[i]);
+      if (ok) return z;
+    }
+    return 0;
+  };
+  if (l.size() >= 2) {
+    const int z = match(l.substr(0, 2));
+    if (z) return z;
+  }
+  return match(l.substr(0, 1));
+}
+
+// Fortran formatted input of one real field (Fw.d / Ew.d): blanks ignored,
+// D or E exponent (or a signed exponent without the letter), and d implied
+// decimals when the field has no point.  An all-blank field reads as 0.
+bool fortran_real(const std::string &field, int d, double &v) {
+  std::string t;
+  for (char c : field)
+    if (c != ' ') t += c;
+  v = 0.0;
+  if (t.empty()) return true;
+  size_t epos = std::string::npos;
+  for (size_t i = 1; i < t.size(); i++) {
+    const char c = t[i];
+    if (c == 'D' || c == 'd' || c == 'E' || c == 'e' || c == 'Q' || c == 'q') { epos = i; break; }
+    if ((c == '+' || c == '-') && t[i - 1] != 'e' && t[i - 1] != 'E' && t[i - 1] != 'd' && t[i - 1] != 'D') {
+      epos = i;
+      break;
+    }
+  }
+  std::string mant = t.substr(0, epos), ex;
+  if (epos != std::string::npos) ex = t.substr(t[epos] == '+' || t[epos] == '-' ? epos : epos + 1);
+  char *end = nullptr;
+  std::strtod(mant.c_str(), &end);
+  if (end == mant.c_str() || *end != '\0') return false;
+  long e10 = 0;
+  if (!ex.empty()) {
+    e10 = std::strtol(ex.c_str(), &end, 10);
+    if (end == ex.c_str() || *end != '\0') return false;
+  }
+  if (mant.find('.') == std::string::npos) e10 -= d;
+  // one correctly rounded conversion of mantissa and exponent together
+  const std::string full = mant + "e" + std::to_string(e10);
+  v = std::strtod(full.c_str(), &end);
+  return *end == '\0';
+}
+
+bool fortran_int(const std::string &field, long &v) {
+  std::string t;
+  for (char c : field)
+    if (c != ' ') t += c;
+  v = 0;
+  if (t.empty()) return true;
+  char *end = nullptr;
+  v = std::strtol(t.c_str(), &end, 10);
+  return end != t.c_str() && *end == '\0';
+}
+
+// Columns [a, a + w) (0-based) of a record padded with blanks.
+std::string col(const std::string &line, size_t a, size_t w) {
+  std::string r = a < line.size() ? line.substr(a, w) : std::string();
+  r.resize(w, ' ');
+  return r;
+}
+
+// Reads n fixed-width fields of a repeated format (skip columns, then up to
+// per fields of width w per record), continuing on new records as Fortran's
+// format reversion does.
+template <class F>
+bool read_fields(std::istream &in, size_t n, size_t skip, size_t per, size_t w, F &&put) {
+  size_t got = 0;
+  std::string line;
+  while (got < n) {
+    if (!std::getline(in, line)) return false;
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    for (size_t k = 0; k < per && got < n; k++, got++)
+      if (!put(got, col(line, skip + k * w, w))) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+// read_wfn (src/wfn_private@proc.F90:981-1118): the AIMPAC wfn format with
+// its fixed columns (formats 101-106 there): header (MO, primitive and
+// nucleus counts), nuclei, centre and type assignments, exponents, any ECP
+// lines up to the first MO record, then per MO its occupation, energy and
+// coefficients.  The wavefunction type follows from the occupations, and a
+// UHF file's alpha count from the first drop of the orbital energy.
+bool read_wfn(const char *path, HostWfn &w, std::string &err) {
+  std::ifstream in(path);
+  if (!in) {
+    err = std::string("cannot open ") + path;
+    return false;
+  }
+  err = std::string("Error reading file: ") + path;
+  std::string line;
+  if (!std::getline(in, line) || !std::getline(in, line)) return false;
+  if (!line.empty() && line.back() == '\r') line.pop_back();
+  long nmo = 0, npri = 0, nat = 0;
+  if (!fortran_int(col(line, 18, 5), nmo) || !fortran_int(col(line, 38, 5), npri) ||
+      !fortran_int(col(line, 58, 5), nat))
+    return false;
+  if (nmo <= 0 || npri <= 0 || nat <= 0) return false;
+  w = HostWfn();
+  w.natom = (int)nat, w.npri = (int)npri, w.nmo = (int)nmo;
+  w.xyz.resize(3 * nat);
+  w.z.resize(nat);
+  for (long a = 0; a < nat; a++) {
+    if (!std::getline(in, line)) return false;
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    for (int j = 0; j < 3; j++)
+      if (!fortran_real(col(line, 24 + 12 * j, 12), 8, w.xyz[3 * a + j])) return false;
+    w.z[a] = zatguess(col(line, 2, 2));
+    if (w.z[a] == 0) {
+      err = "unknown element in " + std::string(path);
+      return false;
+    }
+  }
+  w.icenter.resize(npri);
+  w.itype.resize(npri);
+  w.e.resize(npri);
+  if (!read_fields(in, npri, 20, 20, 3, [&](size_t i, const std::string &f) {
+        long v;
+        if (!fortran_int(f, v)) return false;
+        w.icenter[i] = (int)v - 1;
+        return true;
+      }))
+    return false;
+  if (!read_fields(in, npri, 20, 20, 3, [&](size_t i, const std::string &f) {
+        long v;
+        if (!fortran_int(f, v)) return false;
+        w.itype[i] = (int)v;
+        return true;
+      }))
+    return false;
+  for (int v : w.itype)
+    if (v < 1 || v > 56) {
+      err = "primitive type not supported";
+      return false;
+    }
+  for (int v : w.icenter)
+    if (v < 0 || v >= nat) return false;
+  if (!read_fields(in, npri, 10, 5, 14, [&](size_t i, const std::string &f) { return fortran_real(f, 7, w.e[i]); }))
+    return false;
+  // skip ECP records up to the first one that starts with "MO"
+  std::streampos pos;
+  for (;;) {
+    pos = in.tellg();
+    if (!std::getline(in, line)) return false;
+    if (line.size() >= 2 && line[0] == 'M' && line[1] == 'O') break;
+  }
+  in.seekg(pos);
+  w.occ.resize(nmo);
+  w.cmo.assign((size_t)npri * nmo, 0.0);
+  bool frac = false, found = false;
+  int n1 = 0, n2 = 0, nalpha = -1;
+  double ene0 = -1e30;
+  for (long m = 0; m < nmo; m++) {
+    if (!std::getline(in, line)) return false;
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    double ene = 0.0;
+    if (!fortran_real(col(line, 35, 12), 7, w.occ[m]) || !fortran_real(col(line, 62, 12), 6, ene)) return false;
+    if (!read_fields(in, npri, 0, 5, 16, [&](size_t i, const std::string &f) {
+          return fortran_real(f, 8, w.cmo[i * nmo + m]);
+        }))
+      return false;
+    const long io = std::lround(w.occ[m]);
+    if (std::fabs((double)io - w.occ[m]) > 1e-10) frac = true;
+    else if (io == 1) n1++;
+    else if (io == 2) n2++;
+    if (ene < ene0 - 1e-3) nalpha = (int)m, found = true;
+    ene0 = ene;
+  }
+  if (frac) w.wfntyp = C2G_WFN_FRAC, w.nalpha = 0;
+  else if (n1 == 0) w.wfntyp = C2G_WFN_RHF, w.nalpha = nalpha;
+  else if (n2 == 0) w.wfntyp = C2G_WFN_UHF, w.nalpha = found ? nalpha : (int)nmo;
+  else w.wfntyp = C2G_WFN_ROHF, w.nalpha = n2;
+  err.clear();
+  prune_primitives(w);
+  complete_struct(w);
+  molecular_cell(w);
+  return true;
+}
+
 }  // namespace c2g

@@ -334,3 +334,61 @@ def write_wfx(mol: Molecule, path: str) -> None:
         out += block("EDF Primitive Coefficients", [float(v) for v in mol.edf_c], lambda v: f"{v:.16E}")
     with open(path, "w") as fh:
         fh.write("\n".join(out) + "\n")
+
+
+def _fortran_e(v: float, w: int, d: int, letter: str = "D") -> str:
+    """Fortran Ew.d output with a D exponent: [-]0.ddd...D+ee, right-justified."""
+    if v == 0.0:
+        s = "0." + "0" * d + letter + "+00"
+    else:
+        t = f"{abs(v):.{d - 1}E}"
+        mant, ex = t.split("E")
+        digits = mant.replace(".", "")
+        s = "0." + digits + letter + f"{int(ex) + 1:+03d}"
+        if v < 0:
+            s = "-" + s
+    return s.rjust(w)
+
+
+def round_for_wfn(mol: Molecule) -> Molecule:
+    """The molecule as a wfn file stores it: exponents with 7 and MO
+    coefficients with 8 significant digits, occupations to 1e-7 and
+    coordinates to 1e-8."""
+    r = lambda a, d: np.array([float(_fortran_e(v, 24, d).replace("D", "E")) for v in np.ravel(a)]).reshape(np.shape(a))
+    f = lambda a, d: np.array([float(f"{v:.{d}f}") for v in np.ravel(a)]).reshape(np.shape(a))
+    return dataclasses.replace(mol, e=r(mol.e, 7), cmo=np.ascontiguousarray(r(mol.cmo, 8)),
+                               occ=f(mol.occ, 7), atom_xyz=f(mol.atom_xyz, 8))
+
+
+def write_wfn(mol: Molecule, path: str, energies=None) -> None:
+    """Writes the molecule as an AIMPAC wfn file in the fixed columns that
+    critic2's read_wfn reads (src/wfn_private@proc.F90:1106-1111, formats
+    101-106).  Orbital energies: given, or ascending within each spin block
+    (the beta block of a UHF wavefunction starts lower, which is how
+    read_wfn finds the alpha count)."""
+    sym = {1: "H", 6: "C", 7: "N", 8: "O"}
+    nmo, npri, nat = mol.nmo, mol.npri, mol.natom
+    if energies is None:
+        energies = np.array([-1.0 + 0.01 * m if (mol.wfntyp != 1 or m < mol.nalpha)
+                             else -1.5 + 0.01 * (m - mol.nalpha) for m in range(nmo)])
+    out = [f" synthetic {mol.name}",
+           "GAUSSIAN" + " " * 10 + f"{nmo:5d}" + " MOL ORBITALS  " + f"{npri:5d}" + " PRIMITIVES    "
+           + f"{nat:5d}" + " NUCLEI"]
+    for a in range(nat):
+        x = mol.atom_xyz[a]
+        out.append("  " + f"{sym.get(int(mol.atom_z[a]), 'X'):<2}" + f"{a + 1:4d}    (CENTRE{a + 1:3d}) "
+                   + "".join(f"{v:12.8f}" for v in x) + "  CHARGE =" + f"{float(mol.atom_z[a]):5.1f}")
+    for tag, vals in (("CENTRE ASSIGNMENTS  ", mol.icenter), ("TYPE ASSIGNMENTS    ", mol.itype)):
+        for i in range(0, npri, 20):
+            out.append(tag + "".join(f"{int(v):3d}" for v in vals[i:i + 20]))
+    for i in range(0, npri, 5):
+        out.append("EXPONENTS " + "".join(_fortran_e(v, 14, 7) for v in mol.e[i:i + 5]))
+    for m in range(nmo):
+        head = f"MO{m + 1:5d}     MO 0.0        OCC NO =".ljust(35)[:35]
+        out.append(head + f"{mol.occ[m]:12.7f}" + "  ORB. ENERGY =" + f"{energies[m]:12.6f}")
+        col = mol.cmo[:, m]
+        for i in range(0, npri, 5):
+            out.append("".join(_fortran_e(v, 16, 8) for v in col[i:i + 5]))
+    out.append("END DATA")
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")

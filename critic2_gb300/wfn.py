@@ -58,6 +58,13 @@ class Wavefunction:
         L.check(L.lib().c2g_wfn_read_wfx(path.encode(), C.byref(h)))
         return cls(_handle=h)
 
+    @classmethod
+    def from_wfn(cls, path: str) -> "Wavefunction":
+        """An AIMPAC wfn file (c2g_wfn_read_wfn)."""
+        h = C.c_void_p()
+        L.check(L.lib().c2g_wfn_read_wfn(path.encode(), C.byref(h)))
+        return cls(_handle=h)
+
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
             L.lib().c2g_wfn_destroy(self._h)

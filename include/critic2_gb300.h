@@ -18,8 +18,9 @@
  *   - A handle may be used by one host thread at a time.
  *
  * Reference interfaces replaced (paths within the critic2 source tree):
- *   c2g_wfn_create / c2g_wfn_read_wfx : molwfn%read_wfx + prune_primitives +
- *       complete_struct (src/wfn_private@proc.F90:1121-1284, 3632-3785)
+ *   c2g_wfn_create / c2g_wfn_read_wfx / c2g_wfn_read_wfn : molwfn%read_wfx,
+ *       read_wfn + prune_primitives + complete_struct
+ *       (src/wfn_private@proc.F90:981-1284, 3632-3785)
  *   c2g_rho2      : molwfn%rho2 (src/wfn_private.f90:293-307,
  *                   src/wfn_private@proc.F90:2484-2705), batched over points
  *   c2g_grd       : field%grd for a wavefunction field
@@ -86,6 +87,14 @@ int c2g_wfn_create(int natom, const double *atom_xyz, const int *atom_z, int npr
  * `molecule file.wfx` + `load file.wfx` and creates a handle.  Replaces
  * read_wfx, src/wfn_private@proc.F90:1121-1284. */
 int c2g_wfn_read_wfx(const char *path, c2g_wfn **out);
+
+/* Reads an AIMPAC wfn file (its fixed columns: nuclei, primitives, MOs;
+ * element symbols give the atomic numbers) like critic2's `molecule
+ * file.wfn` + `load file.wfn`, and creates a handle.  RHF/UHF/ROHF/
+ * fractional from the occupations; a UHF file's alpha count from the first
+ * drop of the orbital energies.  Replaces read_wfn,
+ * src/wfn_private@proc.F90:981-1118. */
+int c2g_wfn_read_wfn(const char *path, c2g_wfn **out);
 
 /* Frees the handle and its device memory. */
 int c2g_wfn_destroy(c2g_wfn *h);

@@ -385,3 +385,82 @@ def nci_chk_read(data: bytes, x0, xmat, nstep):
     n = int(np.prod(nstep))
     v = np.frombuffer(r[6][:16 * n])
     return v[:n].copy(), v[n:].copy()
+
+
+# -------------------------------------------------------------- wfn format
+def _fortran_field(s: str, d: int) -> float:
+    t = s.replace(" ", "")
+    if not t:
+        return 0.0
+    t = t.replace("D", "E").replace("d", "E")
+    mant, ex = (t.split("E") + ["0"])[:2] if "E" in t else (t, "0")
+    if "E" not in t:
+        for i in range(1, len(t)):
+            if t[i] in "+-":
+                mant, ex = t[:i], t[i:]
+                break
+    e10 = int(ex) - (0 if "." in mant else d)
+    return float(f"{mant}E{e10}")  # one correctly rounded conversion
+
+
+def read_wfn_text(path: str) -> dict:
+    """read_wfn (src/wfn_private@proc.F90:981-1118) restated on the fixed
+    columns of formats 101-106: returns natom, xyz (natom,3), element labels,
+    icenter/itype (1-based), e, occ, cmo (npri, nmo), energies, wfntyp,
+    nalpha (before prune_primitives)."""
+    lines = open(path).read().split("\n")
+    pad = lambda l, n: l + " " * max(0, n - len(l))
+    h = pad(lines[1], 80)
+    nmo, npri, nat = int(h[18:23]), int(h[38:43]), int(h[58:63])
+    pos = 2
+    xyz, elem = [], []
+    for a in range(nat):
+        l = pad(lines[pos + a], 80)
+        elem.append(l[2:4])
+        xyz.append([_fortran_field(l[24 + 12 * j:36 + 12 * j], 8) for j in range(3)])
+    pos += nat
+
+    def fields(n, skip, per, w, d=0, conv=float):
+        nonlocal pos
+        out = []
+        while len(out) < n:
+            l = pad(lines[pos], skip + per * w)
+            pos += 1
+            for k in range(per):
+                if len(out) == n:
+                    break
+                f = l[skip + k * w:skip + (k + 1) * w]
+                out.append(conv(f) if conv is int else _fortran_field(f, d))
+        return out
+
+    icenter = fields(npri, 20, 20, 3, conv=int)
+    itype = fields(npri, 20, 20, 3, conv=int)
+    e = fields(npri, 10, 5, 14, 7)
+    while not lines[pos].startswith("MO"):
+        pos += 1
+    occ, ene, cmo = [], [], np.zeros((npri, nmo))
+    for m in range(nmo):
+        l = pad(lines[pos], 80)
+        pos += 1
+        occ.append(_fortran_field(l[35:47], 7))
+        ene.append(_fortran_field(l[62:74], 6))
+        cmo[:, m] = fields(npri, 0, 5, 16, 8)
+    frac = any(abs(round(o) - o) > 1e-10 for o in occ)
+    n1 = sum(1 for o in occ if abs(round(o) - o) <= 1e-10 and round(o) == 1)
+    n2 = sum(1 for o in occ if abs(round(o) - o) <= 1e-10 and round(o) == 2)
+    nalpha, found, e0 = -1, False, -1e30
+    for m, en in enumerate(ene):
+        if en < e0 - 1e-3:
+            nalpha, found = m, True
+        e0 = en
+    if frac:
+        typ, na = 3, 0
+    elif n1 == 0:
+        typ, na = 0, nalpha
+    elif n2 == 0:
+        typ, na = 1, (nalpha if found else nmo)
+    else:
+        typ, na = 2, n2
+    return dict(natom=nat, xyz=np.array(xyz), elem=elem, icenter=np.array(icenter, np.int32),
+                itype=np.array(itype, np.int32), e=np.array(e), occ=np.array(occ), cmo=cmo,
+                energies=np.array(ene), wfntyp=typ, nalpha=na)
