@@ -289,113 +289,118 @@ __global__ void __launch_bounds__(NTHR, 1) k_eval_fp64(DevWfn w, Src src, Sink s
 // of the 10 record sums.  GB300's FP64 rate per SM is low, so spreading a
 // handful of points over many SMs is what makes these batches fast; the
 // cutoffs are critic2's exactly, as in k_eval_fp64.
-template <int MPT>
-__global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, IndexSrc src, double *rec) {
+template <int MPT, class Src, class Sink>
+__global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, Src src, Sink sink) {
   constexpr int KC = 256;
   __shared__ double s_chi[KC * 10];
   __shared__ int s_k[KC];
   __shared__ int s_wn[8];
   __shared__ double s_red[8 * kRecNci];
+  __shared__ double s_out[kRecNci];
   const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
-  const int t = blockIdx.x;
-  double x[3];
-  long idx;
-  if (!src.point(w, t / kTilePoints, t % kTilePoints, x, idx)) return;  // uniform per block
-  double acc[MPT][10];
+  for (long t = blockIdx.x;; t += gridDim.x) {  // the list's points, grid-stride
+    double x[3];
+    long idx;
+    if (!src.point(w, (int)(t / kTilePoints), (int)(t % kTilePoints), x, idx)) return;  // uniform per block
+    double acc[MPT][10];
 #pragma unroll
-  for (int m = 0; m < MPT; m++)
+    for (int m = 0; m < MPT; m++)
 #pragma unroll
-    for (int c = 0; c < 10; c++) acc[m][c] = 0.0;
-  for (int k0 = 0; k0 < w.npri; k0 += KC) {
-    const int ip = k0 + tid;
-    double chi[10];
-    bool in = false;
-    if (ip < w.npri) {
-      const PrimF64 pr = w.prim[ip];
-      const double4 A = w.atoms[pr.atom];
-      const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
-      const double dd = dx * dx + dy * dy + dz * dz;
-      if (dd <= A.w) {
-        const double dist = sqrt(dd);
-        if (!(dist > pr.dran)) {
-          in = true;
-          const double ex = exp(-pr.e * (dist * dist));
-          chi_eval<10>(dx, dy, dz, pr.e, pr.lpack, ex, chi);
+      for (int c = 0; c < 10; c++) acc[m][c] = 0.0;
+    for (int k0 = 0; k0 < w.npri; k0 += KC) {
+      const int ip = k0 + tid;
+      double chi[10];
+      bool in = false;
+      if (ip < w.npri) {
+        const PrimF64 pr = w.prim[ip];
+        const double4 A = w.atoms[pr.atom];
+        const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+        const double dd = dx * dx + dy * dy + dz * dz;
+        if (dd <= A.w) {
+          const double dist = sqrt(dd);
+          if (!(dist > pr.dran)) {
+            in = true;
+            const double ex = exp(-pr.e * (dist * dist));
+            chi_eval<10>(dx, dy, dz, pr.e, pr.lpack, ex, chi);
+          }
         }
       }
-    }
-    const unsigned b = __ballot_sync(0xffffffffu, in);
-    if (lane == 0) s_wn[wp] = __popc(b);
-    __syncthreads();
-    int base = 0, nact = 0;
+      const unsigned b = __ballot_sync(0xffffffffu, in);
+      if (lane == 0) s_wn[wp] = __popc(b);
+      __syncthreads();
+      int base = 0, nact = 0;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-      base += i < wp ? s_wn[i] : 0;
-      nact += s_wn[i];
-    }
-    if (in) {
-      const int slot = base + __popc(b & ((1u << lane) - 1u));
+      for (int i = 0; i < 8; i++) {
+        base += i < wp ? s_wn[i] : 0;
+        nact += s_wn[i];
+      }
+      if (in) {
+        const int slot = base + __popc(b & ((1u << lane) - 1u));
 #pragma unroll
-      for (int c = 0; c < 10; c++) s_chi[slot * 10 + c] = chi[c];
-      s_k[slot] = ip;
-    }
-    __syncthreads();
+        for (int c = 0; c < 10; c++) s_chi[slot * 10 + c] = chi[c];
+        s_k[slot] = ip;
+      }
+      __syncthreads();
 #pragma unroll 2
-    for (int j = 0; j < nact; j++) {
-      const double *crow = w.cmo + (size_t)s_k[j] * w.nmo_pad;
-      double ch[10];
+      for (int j = 0; j < nact; j++) {
+        const double *crow = w.cmo + (size_t)s_k[j] * w.nmo_pad;
+        double ch[10];
 #pragma unroll
-      for (int c = 0; c < 10; c++) ch[c] = s_chi[j * 10 + c];
+        for (int c = 0; c < 10; c++) ch[c] = s_chi[j * 10 + c];
 #pragma unroll
-      for (int m = 0; m < MPT; m++) {
-        const int mo = tid + 256 * m;
-        const double cm = mo < w.nmo ? __ldg(crow + mo) : 0.0;
+        for (int m = 0; m < MPT; m++) {
+          const int mo = tid + 256 * m;
+          const double cm = mo < w.nmo ? __ldg(crow + mo) : 0.0;
 #pragma unroll
-        for (int c = 0; c < 10; c++) acc[m][c] = fma(cm, ch[c], acc[m][c]);
+          for (int c = 0; c < 10; c++) acc[m][c] = fma(cm, ch[c], acc[m][c]);
+        }
+      }
+      __syncthreads();
+    }
+    double r[kRecNci];
+#pragma unroll
+    for (int q = 0; q < kRecNci; q++) r[q] = 0.0;
+#pragma unroll
+    for (int m = 0; m < MPT; m++) {
+      const int mo = tid + 256 * m;
+      const double o = mo < w.nmo ? w.occ[mo] : 0.0;
+      const double p0 = acc[m][0], px = acc[m][1], py = acc[m][2], pz = acc[m][3];
+      r[0] += o * p0 * p0;
+      r[1] += 2.0 * o * p0 * px;
+      r[2] += 2.0 * o * p0 * py;
+      r[3] += 2.0 * o * p0 * pz;
+      r[4] += 2.0 * o * (p0 * acc[m][4] + px * px);
+      r[5] += 2.0 * o * (p0 * acc[m][5] + py * py);
+      r[6] += 2.0 * o * (p0 * acc[m][6] + pz * pz);
+      r[7] += 2.0 * o * (p0 * acc[m][7] + px * py);
+      r[8] += 2.0 * o * (p0 * acc[m][8] + px * pz);
+      r[9] += 2.0 * o * (p0 * acc[m][9] + py * pz);
+    }
+#pragma unroll
+    for (int q = 0; q < kRecNci; q++)
+      for (int off = 16; off; off >>= 1) r[q] += __shfl_xor_sync(0xffffffffu, r[q], off);
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < kRecNci; q++) s_red[wp * kRecNci + q] = r[q];
+    __syncthreads();
+    if (wp == 0) {
+      double core_q = 0.0;  // EDF core, component `lane`
+      if (w.nedf) {
+        double core[10];
+        edf_core_warp(w, x, core);
+#pragma unroll
+        for (int q = 0; q < 10; q++)
+          if (q == lane) core_q = core[q];
+      }
+      if (tid < kRecNci) {
+        double sum = 0.0;
+        for (int i = 0; i < 8; i++) sum += s_red[i * kRecNci + tid];
+        s_out[tid] = sum + core_q;
       }
     }
     __syncthreads();
-  }
-  double r[kRecNci];
-#pragma unroll
-  for (int q = 0; q < kRecNci; q++) r[q] = 0.0;
-#pragma unroll
-  for (int m = 0; m < MPT; m++) {
-    const int mo = tid + 256 * m;
-    const double o = mo < w.nmo ? w.occ[mo] : 0.0;
-    const double p0 = acc[m][0], px = acc[m][1], py = acc[m][2], pz = acc[m][3];
-    r[0] += o * p0 * p0;
-    r[1] += 2.0 * o * p0 * px;
-    r[2] += 2.0 * o * p0 * py;
-    r[3] += 2.0 * o * p0 * pz;
-    r[4] += 2.0 * o * (p0 * acc[m][4] + px * px);
-    r[5] += 2.0 * o * (p0 * acc[m][5] + py * py);
-    r[6] += 2.0 * o * (p0 * acc[m][6] + pz * pz);
-    r[7] += 2.0 * o * (p0 * acc[m][7] + px * py);
-    r[8] += 2.0 * o * (p0 * acc[m][8] + px * pz);
-    r[9] += 2.0 * o * (p0 * acc[m][9] + py * pz);
-  }
-#pragma unroll
-  for (int q = 0; q < kRecNci; q++)
-    for (int off = 16; off; off >>= 1) r[q] += __shfl_xor_sync(0xffffffffu, r[q], off);
-  if (lane == 0)
-#pragma unroll
-    for (int q = 0; q < kRecNci; q++) s_red[wp * kRecNci + q] = r[q];
-  __syncthreads();
-  if (wp == 0) {
-    double core_q = 0.0;  // EDF core, component `lane`
-    if (w.nedf) {
-      double core[10];
-      edf_core_warp(w, x, core);
-#pragma unroll
-      for (int q = 0; q < 10; q++)
-        if (q == lane) core_q = core[q];
-    }
-    if (tid < kRecNci) {
-      double sum = 0.0;
-      for (int i = 0; i < 8; i++) sum += s_red[i * kRecNci + tid];
-      rec[idx * kRecNci + tid] = sum + core_q;
-    }
+    if (tid == 0) sink.put(w, idx, x, s_out, 1);
+    __syncthreads();
   }
 }
 
@@ -407,6 +412,19 @@ int num_sms() {
     C2G_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
   }
   return n;
+}
+
+// Per-point form: one block per point, a grid-stride loop over the list
+// (at most 8 blocks per SM), so the launch does not grow with the list's
+// capacity when its length lives on the device.
+template <class Src, class Sink>
+void launch_pt(const DevWfn &w, const Src &src, const Sink &sink, long maxn, cudaStream_t st) {
+  const int grid = (int)std::min<long>(maxn, (long)num_sms() * 8);
+  if (grid <= 0) return;
+  if (w.nmo <= 256) k_eval_fp64_pt<1><<<grid, 256, 0, st>>>(w, src, sink);
+  else if (w.nmo <= 512) k_eval_fp64_pt<2><<<grid, 256, 0, st>>>(w, src, sink);
+  else k_eval_fp64_pt<4><<<grid, 256, 0, st>>>(w, src, sink);
+  C2G_CUDA(cudaGetLastError());
 }
 
 template <class Src, class Sink>
@@ -445,15 +463,11 @@ void launch_fp64_index(const DevWfn &w, const double *d_x, const int *d_idx, con
                        int maxn, double *d_rec, cudaStream_t st) {
   IndexSrc src{d_x, d_idx, d_count};
   if (maxn <= 0) return;
+  RecSink sink{d_rec, kRecNci};
   if (maxn <= kPointKernelMax && w.nmo <= 1024) {
-    // one block per point; blocks past the device count exit at once
-    if (w.nmo <= 256) k_eval_fp64_pt<1><<<maxn, 256, 0, st>>>(w, src, d_rec);
-    else if (w.nmo <= 512) k_eval_fp64_pt<2><<<maxn, 256, 0, st>>>(w, src, d_rec);
-    else k_eval_fp64_pt<4><<<maxn, 256, 0, st>>>(w, src, d_rec);
-    C2G_CUDA(cudaGetLastError());
+    launch_pt(w, src, sink, maxn, st);
     return;
   }
-  RecSink sink{d_rec, kRecNci};
   launch_any(w, 2, false, src, sink, (maxn + TP - 1) / TP, st);
 }
 
@@ -469,6 +483,11 @@ void launch_fp64_nci_list(const DevWfn &w, const GridSpec &g, const int *d_list,
                           int maxn, double *d_crho, double *d_cgrad, cudaStream_t st) {
   GridListSrc src{g, d_list, d_count};
   NciSink sink{d_crho, d_cgrad};
+  if (w.nmo <= 1024) {
+    // scattered re-check points: the per-point form spreads them over all SMs
+    launch_pt(w, src, sink, maxn, st);
+    return;
+  }
   launch_any(w, 2, false, src, sink, (maxn + TP - 1) / TP, st);
 }
 
