@@ -175,7 +175,7 @@ owfn *o_wfn_new(int natom, const double *xyz, const int *z, int npri, int nmo,
   w->nmo = nmo;
   w->icenter = malloc(sizeof(int) * npri);
   w->itype = malloc(sizeof(int) * npri);
-  w->e = malloc(sizeof(double) * npri);
+  w->e = calloc(npri, sizeof(double));
   w->occ = malloc(sizeof(double) * nmo);
   w->cmo = malloc(sizeof(double) * (size_t)npri * nmo);
   for (int i = 0; i < npri; i++) {
