@@ -24,6 +24,7 @@ EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_
            "c2g_autocritic", "c2g_nci_post_dev", "c2g_cube_text", "c2g_dat_text", "c2g_nciplot_files",
            "c2g_grid_field_dev", "c2g_cube_precise_text", "c2g_cube_field_file",
            "c2g_nci_chk_write", "c2g_nci_chk_read", "c2g_cp_graph",
+           "c2g_mesh_size", "c2g_mesh_dev", "c2g_molcalc",
            # learned CP-seed proposer (include/critic2_gb300_cpseed.h)
            "c2g_cs_conv3d", "c2g_cs_conv3d_bwd_data", "c2g_cs_conv3d_bwd_weight", "c2g_cs_loss",
            "c2g_cs_targets", "c2g_cs_features", "c2g_cs_seeds", "c2g_cs_adam")
@@ -47,6 +48,10 @@ class NciCut(C.Structure):
 
 class GraphStats(C.Structure):
     _fields_ = [("npath", C.c_int), ("nbatch", C.c_int), ("nevals", C.c_long), ("ms_total", C.c_double)]
+
+
+class MeshStats(C.Structure):
+    _fields_ = [("npoints", C.c_long), ("ms_mesh", C.c_double), ("ms_total", C.c_double)]
 
 
 class CpReport(C.Structure):
@@ -78,6 +83,9 @@ def lib():
     L.c2g_wfn_destroy.argtypes = [_vp]
     L.c2g_wfn_set_param.argtypes = [_vp, C.c_int, C.c_double]
     L.c2g_wfn_set_edf.argtypes = [_vp, C.c_int, _vp, _vp, _vp, _vp]
+    L.c2g_mesh_size.argtypes = [_vp, C.c_int, C.c_int, C.POINTER(C.c_long)]
+    L.c2g_mesh_dev.argtypes = [_vp, C.c_int, C.c_int, _vp, _vp, _vp]
+    L.c2g_molcalc.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, C.POINTER(MeshStats)]
     L.c2g_cp_graph.argtypes = [_vp, C.c_int, _vp, _vp] + [_vp] * 7 + [C.POINTER(GraphStats)]
     L.c2g_nci_chk_write.argtypes = [C.c_char_p, _dp, _dp, _ip, _dp, _dp]
     L.c2g_nci_chk_read.argtypes = [C.c_char_p, _dp, _dp, _ip, _dp, _dp, C.POINTER(C.c_int)]

@@ -139,8 +139,10 @@ struct GridSpec {
 };
 
 // k_fp64.cu
+// wrap = false evaluates the points as given, as grd does for a molecule
+// with periodic = .false. (molecular meshes).
 void launch_fp64_points(const DevWfn &w, int n, const double *d_xyz, int nder, bool full,
-                        double *d_rec, cudaStream_t st);
+                        double *d_rec, cudaStream_t st, bool wrap = true);
 // kRecNci records of the points x(3, idx[t]), t < *count, written at rec[t].
 void launch_fp64_index(const DevWfn &w, const double *d_x, const int *d_idx, const int *d_count,
                        int maxn, double *d_rec, cudaStream_t st);

@@ -453,8 +453,8 @@ void launch_any(const DevWfn &w, int nder, bool full, const Src &src, const Sink
 }  // namespace
 
 void launch_fp64_points(const DevWfn &w, int n, const double *d_xyz, int nder, bool full,
-                        double *d_rec, cudaStream_t st) {
-  ListSrc src{d_xyz, n};
+                        double *d_rec, cudaStream_t st, bool wrap) {
+  ListSrc src{d_xyz, n, wrap};
   RecSink sink{d_rec, full ? kRecFull : kRecNci};
   launch_any(w, nder, full, src, sink, (n + TP - 1) / TP, st);
 }

@@ -1389,10 +1389,10 @@ void tc_set_recheck(Handle &h, double rel) { h.tc->recheck_rel = rel; }
 
 void tc_check_error(Handle &h) { check_device_error(h.tc); }
 
-void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st) {
+void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st, bool wrap) {
   const int kind = kind_of(prec);
   TcArgs a = make_args(h, kind);
-  ListSrc src{d_xyz, n};
+  ListSrc src{d_xyz, n, wrap};
   launch_kind(kind, a, src, TcRecSink{d_rec}, (n + 31) / 32, st);
   C2G_CUDA(cudaStreamSynchronize(st));
   check_device_error(h.tc);

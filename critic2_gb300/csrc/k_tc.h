@@ -17,7 +17,8 @@ void tc_set_recheck(Handle &h, double rel);
 void tc_check_error(Handle &h);
 
 // kRecNci records (rho, grad, hess) at n device points, split precision.
-void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st);
+void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, cudaStream_t st,
+               bool wrap = true);
 
 // kRecNci records of the points x(3, idx[t]), t < *d_count (<= maxn), split
 // precision, written at rec[t].

@@ -28,6 +28,7 @@ __device__ __forceinline__ void wrap_cell(const DevWfn &w, double (&x)[3]) {
 struct ListSrc {
   const double *xyz;
   int n;
+  bool wrap = true;  // false: the points as given (grd with periodic = .false.)
   __device__ int tiles(int nt) const { return nt; }
   __device__ bool point(const DevWfn &w, int tile, int p, double (&x)[3], long &idx) const {
     const long i = (long)tile * kTilePoints + p;
@@ -36,7 +37,7 @@ struct ListSrc {
     x[0] = xyz[3 * i];
     x[1] = xyz[3 * i + 1];
     x[2] = xyz[3 * i + 2];
-    wrap_cell(w, x);
+    if (wrap) wrap_cell(w, x);
     return true;
   }
 };

@@ -207,6 +207,37 @@ class Wavefunction:
         L.check(L.lib().c2g_pair_seeds(self._h, maxdist, npts, L.ptr(buf), C.byref(n)))
         return buf[: n.value]
 
+    MESH_TYPES = {"becke": 1, "franchini": 2}
+    MESH_LEVELS = {"small": 1, "normal": 2, "good": 3, "vgood": 4, "amazing": 5}
+    MOLCALC = {"volume": 0, "rho": 1, "gradrho": 2, "gkin": 3}
+
+    def mesh_size(self, mesh="franchini", level="good") -> int:
+        n = C.c_long(0)
+        L.check(L.lib().c2g_mesh_size(self._h, self.MESH_TYPES[mesh], self.MESH_LEVELS[level], C.byref(n)))
+        return n.value
+
+    def mesh(self, mesh="franchini", level="good"):
+        """The integration mesh (c2g_mesh_dev) as host arrays xyz (n,3), w (n,)."""
+        import torch
+        n = self.mesh_size(mesh, level)
+        x = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        w = torch.empty(n, dtype=torch.float64, device="cuda")
+        L.check(L.lib().c2g_mesh_dev(self._h, self.MESH_TYPES[mesh], self.MESH_LEVELS[level],
+                                     C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()), None))
+        return x.cpu().numpy(), w.cpu().numpy()
+
+    def molcalc(self, quantities=("rho",), mesh="franchini", level="good", prec="fp64") -> dict:
+        """Mesh integrals (c2g_molcalc): {quantity: integral} plus npoints
+        and the wall times."""
+        q = _i32([self.MOLCALC[k] for k in quantities])
+        out = np.zeros(len(q))
+        st = L.MeshStats()
+        L.check(L.lib().c2g_molcalc(self._h, self.MESH_TYPES[mesh], self.MESH_LEVELS[level], _prec(prec),
+                                    len(q), L.ptr(q), L.ptr(out), C.byref(st)))
+        r = {k: float(v) for k, v in zip(quantities, out)}
+        r.update(npoints=st.npoints, ms_mesh=st.ms_mesh, ms_total=st.ms_total)
+        return r
+
     def cp_graph(self, cp_xyz, cp_typ) -> dict:
         """makegraph over a CP list (c2g_cp_graph): ipath (n,2) 1-based
         terminator indices (0 none, -1 outside), brdist (n,2), brpathlen

@@ -268,6 +268,46 @@ int c2g_nci_chk_write(const char *path, const double *x0, const double *xmat, co
 int c2g_nci_chk_read(const char *path, const double *x0, const double *xmat, const int *nstep, double *crho,
                      double *cgrad, int *found);
 
+/* Molecular integration meshes (src/meshmod@proc.f90:45-627): atom-centred
+ * radial x Lebedev angular grids with Becke's or Franchini's partition of
+ * space, in critic2's point order (atoms, radial shells, angular points).
+ * Becke: rmesh_postg radial grid, Becke's fuzzy cells (four smoothing
+ * iterations, no size adjustment).  Franchini (critic2's default): Gauss-
+ * Legendre radial grid scaled by the tabulated zeta(Z), weights from
+ * f exp(-2 d)/d^3 (f = 0.3 for H) over the atoms within max(r_max, 12 bohr).
+ * Levels set the radial counts (z2nr) and Lebedev sizes 110, 194, 302, 590,
+ * 770 (z2nang); the default is good (302).  Lattice images of the atoms,
+ * which critic2's molecular cell adds to the partition of points farther
+ * than the cell border, are not included (those points carry no density). */
+#define C2G_MESH_BECKE 1
+#define C2G_MESH_FRANCHINI 2
+#define C2G_MESH_SMALL 1
+#define C2G_MESH_NORMAL 2
+#define C2G_MESH_GOOD 3
+#define C2G_MESH_VGOOD 4
+#define C2G_MESH_AMAZING 5
+/* quantities integrated by c2g_molcalc (fillmesh's im_*) */
+#define C2G_MOLCALC_VOLUME 0  /* 1 */
+#define C2G_MOLCALC_RHO 1     /* rho (molcalc_nelec, molcalc "$1") */
+#define C2G_MOLCALC_GRADRHO 2 /* |grad rho| */
+#define C2G_MOLCALC_GKIN 3    /* kinetic energy density G (FP64 only) */
+
+typedef struct {
+  long npoints;    /* mesh points */
+  double ms_mesh;  /* building the mesh on the GPU */
+  double ms_total; /* the whole call */
+} c2g_mesh_stats;
+
+/* Number of points of the mesh (genmesh's m%n). */
+int c2g_mesh_size(const c2g_wfn *h, int type, int level, long *npoints);
+/* The mesh into caller device buffers d_xyz(3, n) and d_w(n) (genmesh). */
+int c2g_mesh_dev(c2g_wfn *h, int type, int level, double *d_xyz, double *d_w, void *stream);
+/* molcalc: integral(q) = sum_i w_i f_q(x_i) over the mesh for nq quantities
+ * (fillmesh + molcalc_nelec / molcalc_expression, src/molcalc@proc.F90:
+ * 94-256), the field evaluated in precision prec.  stats may be NULL. */
+int c2g_molcalc(c2g_wfn *h, int type, int level, int prec, int nq, const int *quant, double *integral,
+                c2g_mesh_stats *stats);
+
 /* Quantities of field%grd for CUBE plots (rhoplot_cube's nti selectors,
  * src/rhoplot@proc.f90:905-930). */
 #define C2G_FIELD_RHO 0

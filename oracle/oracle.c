@@ -1125,6 +1125,173 @@ void o_makegraph(const owfn *w, int ncp, const double *cpx, const int *cptyp, in
   }
 }
 
+/* ------------------------------------------------------ molecular meshes */
+/* genmesh_becke / genmesh_franchini, src/meshmod@proc.f90:79-371, and the
+ * radial helpers :508-627, for a molecule without lattice images.  The
+ * angular rule (nang points x, y, z, w with w summing to 1) is given by the
+ * caller.  Output in critic2's order: atoms, radial shells, angular points. */
+static const double O_ZETA[103] = {
+    0.8, 0.9, 1.8, 1.4, 1.3, 1.1, 0.9, 0.9, 0.9, 0.9, 1.4, 1.3, 1.3, 1.2, 1.1, 1.0, 1.0, 1.0, 1.5, 1.4,
+    1.3, 1.2, 1.2, 1.2, 1.2, 1.2, 1.2, 1.1, 1.1, 1.1, 1.1, 1.0, 0.9, 0.9, 0.9, 0.9, 1.4, 1.4, 1.1, 1.3,
+    1.0, 1.2, 0.9, 0.9, 0.9, 1.0, 0.9, 1.0, 1.0, 1.3, 1.2, 1.2, 0.9, 1.0, 1.7, 1.5, 1.5, 1.3, 1.3, 1.4,
+    1.8, 1.4, 1.2, 1.3, 1.3, 1.4, 1.1, 1.1, 1.2, 1.6, 1.4, 1.3, 1.2, 1.0, 1.0, 0.9, 1.3, 1.2, 1.2, 1.0,
+    1.2, 1.2, 1.1, 1.2, 1.1, 2.1, 2.2, 1.8, 1.7, 1.3, 1.4, 1.2, 1.2, 1.3, 1.4, 1.4, 1.7, 1.9, 1.9, 2.0,
+    2.0, 1.6, 2.0};
+
+int o_z2nr(int z, int lvl) {
+  int nr = 15;
+  if (z > 2) nr = 20;
+  if (z > 10) nr = 25;
+  if (z > 18) nr = 35;
+  if (z > 36) nr = 60;
+  if (z > 54) nr = 85;
+  if (z > 86) nr = 110;
+  /* default-kind (single precision) literals in critic2 */
+  static const float f[6] = {0.f, 2.37f, 3.08f, 3.42f, 4.27f, 6.72f};
+  return (int)ceilf((float)nr * f[lvl]);
+}
+
+/* gauleg on (-1, 1): ascending nodes, Newton on the Legendre recurrence */
+static void o_gauleg(int n, double *x, double *w) {
+  for (int i = 1; i <= (n + 1) / 2; i++) {
+    double z = cos(M_PI * (i - 0.25) / (n + 0.5)), pp = 0.0, z1;
+    do {
+      double p1 = 1.0, p2 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      z1 = z;
+      z = z1 - p1 / pp;
+    } while (fabs(z - z1) > 1e-15);
+    x[i - 1] = -z;
+    x[n - i] = z;
+    w[i - 1] = w[n - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+  }
+}
+
+static void o_radial(int type, int n, int z, double *r, double *wr) {
+  const double fourpi = 4.0 * M_PI;
+  if (type == 1) { /* rmesh_postg */
+    double rmid = 1.0 / pow((double)z, 1.0 / 3.0), h = 1.0 / (n + 1);
+    for (int i = 1; i <= n; i++) {
+      double q = h * i;
+      r[i - 1] = rmid * q / (1.0 - q);
+      wr[i - 1] = fourpi * h * r[i - 1] * r[i - 1] * rmid / ((1.0 - q) * (1.0 - q));
+    }
+  } else { /* rmesh_franchini */
+    double *q = malloc(sizeof(double) * n), *wq = malloc(sizeof(double) * n);
+    o_gauleg(n, q, wq);
+    double zeta = O_ZETA[z - 1], l2 = log(2.0);
+    for (int i = 0; i < n; i++) {
+      double l = log(2.0 / (1.0 - q[i]));
+      r[i] = zeta / l2 * (1.0 + q[i]) * l;
+      wr[i] = fourpi * r[i] * r[i] * wq[i] * zeta / l2 * (l + (1.0 + q[i]) / (1.0 - q[i]));
+    }
+    free(q);
+    free(wq);
+  }
+}
+
+long o_mesh_size(const owfn *w, int lvl, int nang) {
+  long n = 0;
+  for (int a = 0; a < w->natom; a++) n += (long)o_z2nr(w->z[a], lvl) * nang;
+  return n;
+}
+
+void o_mesh(const owfn *w, int type, int lvl, int nang, const double *ang, double *xyz, double *wt,
+            int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  int na = w->natom;
+  long *off = malloc(sizeof(long) * (na + 1));
+  off[0] = 0;
+  for (int a = 0; a < na; a++) off[a + 1] = off[a] + (long)o_z2nr(w->z[a], lvl) * nang;
+  double rmax = 0.0, *rr = NULL;
+  if (type == 2) {
+    int mr = -1, izmr = -1;
+    for (int a = 0; a < na; a++) {
+      int nr = o_z2nr(w->z[a], lvl);
+      if (nr > mr || (nr == mr && w->z[a] > izmr)) mr = nr, izmr = w->z[a];
+    }
+    double *r = malloc(sizeof(double) * mr), *wr = malloc(sizeof(double) * mr);
+    o_radial(2, mr, izmr, r, wr);
+    rmax = fmax(r[mr - 1], 12.0);
+    free(r);
+    free(wr);
+  } else {
+    rr = calloc((size_t)na * na, sizeof(double));
+    for (int i = 0; i < na; i++)
+      for (int j = i + 1; j < na; j++) {
+        const double *a = w->xyz + 3 * i, *b = w->xyz + 3 * j;
+        rr[(size_t)i * na + j] = rr[(size_t)j * na + i] =
+            sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+      }
+  }
+#pragma omp parallel for schedule(dynamic)
+  for (int i = 0; i < na; i++) {
+    int nr = o_z2nr(w->z[i], lvl);
+    double *r = malloc(sizeof(double) * nr), *wr = malloc(sizeof(double) * nr);
+    double *cut = type == 1 ? malloc(sizeof(double) * (size_t)na * na) : NULL;
+    o_radial(type, nr, w->z[i], r, wr);
+    double fscal = w->z[i] == 1 ? 0.3 : 1.0;
+    const double *c = w->xyz + 3 * i;
+    for (int ir = 0; ir < nr; ir++) {
+      double vp0f = fscal * exp(-2.0 * r[ir]) / pow(fmax(r[ir], 1e-10), 3);
+      for (int il = 0; il < nang; il++) {
+        long p = off[i] + (long)ir * nang + il;
+        double x[3];
+        for (int k = 0; k < 3; k++) x[k] = c[k] + r[ir] * ang[4 * il + k];
+        double part;
+        if (type == 2) {
+          double vpsum = 0.0;
+          for (int j = 0; j < na; j++) {
+            const double *b = w->xyz + 3 * j;
+            double dd = (x[0] - b[0]) * (x[0] - b[0]) + (x[1] - b[1]) * (x[1] - b[1]) + (x[2] - b[2]) * (x[2] - b[2]);
+            if (!(dd <= rmax * rmax)) continue;
+            double d = sqrt(dd), dm = fmax(d, 1e-10);
+            vpsum += (w->z[j] == 1 ? 0.3 : 1.0) * exp(-2.0 * d) / (dm * dm * dm);
+          }
+          vpsum = fmax(vp0f, vpsum);
+          part = vp0f / fmax(vpsum, 1e-40);
+        } else {
+          for (int j = 1; j < na; j++) {
+            for (int k = 0; k < j; k++) {
+              const double *bj = w->xyz + 3 * j, *bk = w->xyz + 3 * k;
+              double r1 = sqrt((x[0] - bj[0]) * (x[0] - bj[0]) + (x[1] - bj[1]) * (x[1] - bj[1]) + (x[2] - bj[2]) * (x[2] - bj[2]));
+              double r2 = sqrt((x[0] - bk[0]) * (x[0] - bk[0]) + (x[1] - bk[1]) * (x[1] - bk[1]) + (x[2] - bk[2]) * (x[2] - bk[2]));
+              double h = (r1 - r2) / rr[(size_t)j * na + k];
+              for (int it = 0; it < 4; it++) h = 1.5 * h - 0.5 * h * h * h;
+              cut[(size_t)j * na + k] = (1.0 - h) / 2.0;
+              cut[(size_t)k * na + j] = (1.0 + h) / 2.0;
+            }
+            cut[(size_t)j * na + j] = 1.0;
+          }
+          cut[0] = 1.0;
+          double vp0 = 1.0, vpsum = 0.0;
+          for (int j = 0; j < na; j++) {
+            vp0 *= cut[(size_t)i * na + j];
+            double vpi = 1.0;
+            for (int k = 0; k < na; k++) vpi *= cut[(size_t)j * na + k];
+            vpsum += vpi;
+          }
+          part = vp0 / vpsum;
+        }
+        for (int k = 0; k < 3; k++) xyz[3 * p + k] = x[k];
+        wt[p] = part * wr[ir] * ang[4 * il + 3];
+      }
+    }
+    free(r);
+    free(wr);
+    free(cut);
+  }
+  free(off);
+  free(rr);
+}
+
 /* ------------------------------------------------------------ NCI output */
 /* Fortran list output of (" ",1p,e13.5e3): blank, then the number right-
  * justified in 13 columns with 6 significant digits and a 3-digit

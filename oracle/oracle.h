@@ -100,6 +100,13 @@ int o_gradient(const owfn *w, double x[3], int iup, int ncp, const double *cpx, 
 void o_makegraph(const owfn *w, int ncp, const double *cpx, const int *cptyp, int *ipath, double *brdist,
                  double *brpathlen, double *brang, double *brvec, int *ier, int *nstep, int nthreads);
 
+/* Molecular meshes (src/meshmod@proc.f90:79-627): type 1 Becke, 2
+ * Franchini; ang(4, nang) the angular rule (weights sum to 1). */
+int o_z2nr(int z, int lvl);
+long o_mesh_size(const owfn *w, int lvl, int nang);
+void o_mesh(const owfn *w, int type, int lvl, int nang, const double *ang, double *xyz, double *wt,
+            int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

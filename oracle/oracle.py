@@ -77,6 +77,11 @@ def lib():
                                  C.POINTER(C.c_double)]
         L.o_gradient.restype = C.c_int
         L.o_makegraph.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, C.c_int]
+        L.o_z2nr.argtypes = [C.c_int, C.c_int]
+        L.o_z2nr.restype = C.c_int
+        L.o_mesh_size.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.o_mesh_size.restype = C.c_long
+        L.o_mesh.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int]
         L.o_fmt_e13_5e3.argtypes = [C.c_double, C.c_char_p]
         L.o_fmt_E15_7.argtypes = [C.c_double, C.c_char_p]
         L.o_fmt_E22_14E3.argtypes = [C.c_double, C.c_char_p]
@@ -202,6 +207,43 @@ class Wfn:
         lib().o_makegraph(self.h, n, _f64(cp_xyz).reshape(-1), ct, out["ipath"].reshape(-1),
                           out["brdist"].reshape(-1), out["brpathlen"].reshape(-1), out["brang"],
                           out["brvec"].reshape(-1), out["ier"].reshape(-1), out["nstep"].reshape(-1), nthreads)
+        return out
+
+    def mesh(self, mesh="franchini", level="good", nthreads=0):
+        """genmesh: (xyz (n,3), w (n,)) with the Lebedev rules of
+        tests/golden/lebedev_rules.json."""
+        t = {"becke": 1, "franchini": 2}[mesh]
+        lvl = {"small": 1, "normal": 2, "good": 3, "vgood": 4, "amazing": 5}[level]
+        nang = (0, 110, 194, 302, 590, 770)[lvl]
+        ang = _f64(lebedev_rule(nang)).reshape(-1)
+        n = lib().o_mesh_size(self.h, lvl, nang)
+        xyz, wt = np.zeros(3 * n), np.zeros(n)
+        lib().o_mesh(self.h, t, lvl, nang, ang, xyz, wt, nthreads)
+        return xyz.reshape(n, 3), wt
+
+    def molcalc(self, quantities=("rho",), mesh="franchini", level="good", nthreads=0):
+        """molcalc: sum_i w_i f(x_i) for rho, gradrho (|grad rho|), volume."""
+        xyz, wt = self.mesh(mesh, level, nthreads)
+        # fillmesh evaluates a molecule with periodic = .false. (no wrap),
+        # src/molcalc@proc.F90:113
+        need = any(q != "volume" for q in quantities)
+        rho, grad = self.rho2_points(xyz, 1, nthreads)[:2] if need else (None, None)
+        out = {}
+        for q in quantities:
+            if q == "volume":
+                f = np.ones(len(wt))
+            elif q == "rho":
+                f = rho
+            elif q == "gradrho":
+                g = grad.reshape(-1, 3).copy()
+                # nucleus rule of grd: |grad| := 0 within 1e-5 bohr of a nucleus
+                for a in self.mol.atom_xyz:
+                    g[np.linalg.norm(xyz - a, axis=1) <= 1e-5] = 0.0
+                f = np.linalg.norm(g, axis=1)
+            else:
+                raise ValueError(q)
+            out[q] = float(np.sum(f * wt))
+        out["npoints"] = len(wt)
         return out
 
     def autocritic(self, seeds=None, nthreads=0):
@@ -464,3 +506,18 @@ def read_wfn_text(path: str) -> dict:
     return dict(natom=nat, xyz=np.array(xyz), elem=elem, icenter=np.array(icenter, np.int32),
                 itype=np.array(itype, np.int32), e=np.array(e), occ=np.array(occ), cmo=cmo,
                 energies=np.array(ene), wfntyp=typ, nalpha=na)
+
+
+_LEBEDEV = None
+
+
+def lebedev_rule(n: int) -> np.ndarray:
+    """The n-point Lebedev rule (n, 4): x, y, z, weight (sum 1), from the
+    committed fixture tests/golden/lebedev_rules.json."""
+    global _LEBEDEV
+    if _LEBEDEV is None:
+        import json
+        here = os.path.dirname(os.path.abspath(__file__))
+        with open(os.path.join(here, "..", "tests", "golden", "lebedev_rules.json")) as fh:
+            _LEBEDEV = {int(k): np.array(v) for k, v in json.load(fh).items()}
+    return _LEBEDEV[n]
