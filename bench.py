@@ -163,6 +163,14 @@ def run_reference(args, wl, mol):
                                                 "nciplot loop (reference Fortran unbuildable here)"},
             "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    if not args.no_mesh:
+        from oracle import oracle as _o
+        ow = _o.Wfn(mol)
+        t0 = time.perf_counter()
+        r = ow.molcalc(("rho",), "franchini", "good", nthreads=threads)
+        line["molcalc"] = {"mesh": "franchini, good", "quantity": "integral of rho", "unit": "ms",
+                           "ms": 1e3 * (time.perf_counter() - t0), "integral": r["rho"], "npoints": r["npoints"],
+                           "cores": threads, "kind": "port"}
     if not args.no_cp:
         # the metric's second part on the CPU: AUTO with critic2's pair seeds
         # on the 100-atom molecule, all host threads
@@ -230,6 +238,7 @@ def main():
     ap.add_argument("--binned", action="store_true", help="FP64 comparison binned by rho decade")
     ap.add_argument("--no-cp", action="store_true", help="skip the CP-search part")
     ap.add_argument("--no-files", action="store_true", help="skip the cube/dat output part")
+    ap.add_argument("--no-mesh", action="store_true", help="skip the molcalc mesh-integral part")
     ap.add_argument("--fp64-planes", type=int, default=0, help="FP64 comparison on this many i-planes")
     ap.add_argument("--cp-modes", default="fp64:0,fp64:30,tf32x3:30",
                     help="CP-search precision:stall pairs (stall 0 = critic2's Newton)")
@@ -397,6 +406,17 @@ def main():
         line["nci_files"] = {"ms_evaluation": parts[0], "ms_cutoff_pass": parts[1], "ms_text": parts[2],
                              "ms_write": parts[3], "bytes": sizes,
                              "note": "text formatted on the GPU (correctly rounded, near ties on the host)"}
+    if rank == 0 and not args.no_mesh:
+        # molcalc: the integral of rho over critic2's default molecular mesh
+        # (Franchini, good), mesh built and field evaluated on the GPU
+        mc = {"mesh": "franchini, good", "quantity": "integral of rho", "unit": "ms"}
+        for p_ in ("fp64", "tf32x3"):
+            w.molcalc(("rho",), "franchini", "good", p_)  # warm-up
+            t0 = time.perf_counter()
+            r = w.molcalc(("rho",), "franchini", "good", p_)
+            mc[p_] = {"ms": 1e3 * (time.perf_counter() - t0), "integral": r["rho"], "ms_mesh": r["ms_mesh"]}
+            mc["npoints"] = r["npoints"]
+        line["molcalc"] = mc
     if rank == 0 and not args.no_cp:
         cps = cp_search(args)
         if cps:
