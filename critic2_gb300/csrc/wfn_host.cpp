@@ -13,6 +13,7 @@
 #include <sstream>
 
 #include "c2g_internal.h"
+#include "sphcar_tables.h"
 
 namespace c2g {
 
@@ -492,6 +493,226 @@ bool read_wfn(const char *path, HostWfn &w, std::string &err) {
   else if (n1 == 0) w.wfntyp = C2G_WFN_RHF, w.nalpha = nalpha;
   else if (n2 == 0) w.wfntyp = C2G_WFN_UHF, w.nalpha = found ? nalpha : (int)nmo;
   else w.wfntyp = C2G_WFN_ROHF, w.nalpha = n2;
+  err.clear();
+  prune_primitives(w);
+  complete_struct(w);
+  molecular_cell(w);
+  return true;
+}
+
+// ----------------------------------------------------------------- fchk
+namespace {
+
+// Normalisation of a Cartesian primitive x^a y^b z^c exp(-al r^2) (gnorm,
+// src/wfn_private@proc.F90:3375-3459, in closed form).
+double gnorm_cart(const int *l, double al) {
+  const int L = l[0] + l[1] + l[2];
+  double df = 1.0;
+  for (int k = 0; k < 3; k++)
+    for (int v = 2 * l[k] - 1; v > 1; v -= 2) df *= v;
+  return std::pow(2.0, (4.0 * L + 3.0) / 4.0) * std::pow(al, (2.0 * L + 3.0) / 4.0) /
+         std::pow(M_PI, 0.75) / std::sqrt(df);
+}
+
+// Normalisation of a contracted Cartesian function with coefficients c of
+// normalised primitives (aonorm, :3461-3540).
+double aonorm_cart(const int *l, int n, const double *a, const double *c) {
+  const int L = l[0] + l[1] + l[2];
+  double df = 1.0;
+  for (int k = 0; k < 3; k++)
+    for (int v = 2 * l[k] - 1; v > 1; v -= 2) df *= v;
+  double s = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) s += c[i] * c[j] / std::pow(a[i] + a[j], L + 1.5);
+  s *= df * std::pow(M_PI, 1.5) / std::pow(2.0, L);
+  return 1.0 / std::sqrt(s);
+}
+
+// fchk Cartesian components of a shell of angular momentum l, as critic2
+// li types (the order of Gaussian's checkpoint files)
+std::vector<int> fchk_cart_types(int l) {
+  static const char *const ord[5][15] = {
+      {"", 0},
+      {"x", "y", "z"},
+      {"xx", "yy", "zz", "xy", "xz", "yz"},
+      {"xxx", "yyy", "zzz", "xyy", "xxy", "xxz", "xzz", "yzz", "yyz", "xyz"},
+      {"zzzz", "yzzz", "yyzz", "yyyz", "yyyy", "xzzz", "xyzz", "xyyz", "xyyy", "xxzz", "xxyz", "xxyy", "xxxz",
+       "xxxy", "xxxx"}};
+  static const int n[5] = {1, 3, 6, 10, 15};
+  std::vector<int> t;
+  for (int i = 0; i < n[l]; i++) {
+    int e[3] = {0, 0, 0};
+    for (const char *c = ord[l][i]; c && *c; c++) e[*c - 'x']++;
+    for (int k = 0; k < 56; k++)
+      if (kLi[k][0] == e[0] && kLi[k][1] == e[1] && kLi[k][2] == e[2]) {
+        t.push_back(k + 1);
+        break;
+      }
+  }
+  return t;
+}
+
+}  // namespace
+
+// read_fchk (src/wfn_private@proc.F90:1287-1812) without virtual orbitals:
+// the occupied MOs of a Gaussian formatted checkpoint, sp shells unfolded,
+// pure d/f/g shells transformed to Cartesian Gaussians (real solid
+// harmonics in Gaussian's m = 0, 1, -1, ... order), every Cartesian
+// component normalised with its own primitive and contraction factors.
+bool read_fchk(const char *path, HostWfn &w, std::string &err) {
+  std::ifstream in(path);
+  if (!in) {
+    err = std::string("cannot open ") + path;
+    return false;
+  }
+  err = std::string("Error reading file: ") + path;
+  std::vector<std::string> lines;
+  for (std::string l; std::getline(in, l);) {
+    if (!l.empty() && l.back() == '\r') l.pop_back();
+    lines.push_back(l);
+  }
+  auto starts = [](const std::string &l, const char *key) { return l.compare(0, std::strlen(key), key) == 0; };
+  auto last_int = [](const std::string &l, long &v) {
+    std::istringstream ss(l);
+    std::string tok, lastt;
+    while (ss >> tok) lastt = tok;
+    char *end = nullptr;
+    v = std::strtol(lastt.c_str(), &end, 10);
+    return end != lastt.c_str() && *end == '\0';
+  };
+  long nelec = 0, nalpha = 0, nbeta = 0, nbas = 0, ncshel = 0, nshel = 0, natom = 0, nmoa = 0;
+  bool uhf = false;
+  for (const std::string &l : lines) {
+    long v = 0;
+    if (starts(l, "Number of electrons") && last_int(l, v)) nelec = v;
+    else if (starts(l, "Number of alpha electrons") && last_int(l, v)) nalpha = v;
+    else if (starts(l, "Number of beta electrons") && last_int(l, v)) nbeta = v;
+    else if (starts(l, "Number of basis functions") && last_int(l, v)) nbas = v;
+    else if (starts(l, "Number of contracted shells") && last_int(l, v)) ncshel = v;
+    else if (starts(l, "Number of primitive shells") && last_int(l, v)) nshel = v;
+    else if (starts(l, "Atomic numbers") && last_int(l, v)) natom = v;
+    else if (starts(l, "Alpha Orbital Energies") && last_int(l, v)) nmoa = v;
+    else if (starts(l, "Beta Orbital Energies")) uhf = true;
+  }
+  if (nelec == 0) { err = "nelec = 0 reading fchk file"; return false; }
+  if (nmoa == 0) { err = "nmoall = 0 reading fchk file"; return false; }
+  if (ncshel <= 0 || nshel <= 0 || nbas <= 0 || natom <= 0) return false;
+  int wfntyp, nmoocc, nalf;
+  if (uhf) wfntyp = C2G_WFN_UHF, nmoocc = (int)nelec, nalf = (int)nalpha;
+  else if (nalpha == nbeta) wfntyp = C2G_WFN_RHF, nmoocc = (int)(nelec / 2), nalf = (int)(nelec / 2);
+  else wfntyp = C2G_WFN_ROHF, nmoocc = (int)nalpha, nalf = (int)nbeta;
+  const int namo = wfntyp == C2G_WFN_ROHF ? nmoocc : nalf;  // alpha MOs read
+  // array sections: the values after a "Name  X  N=  n" line
+  auto section = [&](const char *key, size_t n, std::vector<double> &out) {
+    out.clear();
+    for (size_t i = 0; i < lines.size(); i++) {
+      if (!starts(lines[i], key)) continue;
+      for (size_t j = i + 1; j < lines.size() && out.size() < n; j++) {
+        std::istringstream ss(lines[j]);
+        std::string tok;
+        while (out.size() < n && ss >> tok) {
+          for (char &c : tok)
+            if (c == 'D' || c == 'd') c = 'E';
+          char *end = nullptr;
+          const double v = std::strtod(tok.c_str(), &end);
+          if (end == tok.c_str() || *end != '\0') return false;
+          out.push_back(v);
+        }
+      }
+      return out.size() == n;
+    }
+    return false;
+  };
+  std::vector<double> zs, xyz, st, np_, sa, ex, cc, pc, moa, mob;
+  if (!section("Atomic numbers", natom, zs) || !section("Current cartesian coordinates", 3 * natom, xyz) ||
+      !section("Shell types", ncshel, st) || !section("Number of primitives per shell", ncshel, np_) ||
+      !section("Shell to atom map", ncshel, sa) || !section("Primitive exponents", nshel, ex) ||
+      !section("Contraction coefficients", nshel, cc))
+    return false;
+  bool has_sp = false;
+  for (double t : st) has_sp = has_sp || (int)t == -1;
+  if (has_sp && !section("P(S=P) Contraction coefficients", nshel, pc)) return false;
+  if (!section("Alpha MO coefficients", (size_t)namo * nbas, moa)) return false;
+  if (nmoocc > namo && !section("Beta MO coefficients", (size_t)(nmoocc - namo) * nbas, mob)) return false;
+  // unfold sp shells: (type, nprim, atom, exponents, coefficients)
+  struct Shell {
+    int type, atom;
+    std::vector<double> a, c;
+  };
+  std::vector<Shell> sh;
+  size_t off = 0;
+  for (long i = 0; i < ncshel; i++) {
+    const int t = (int)st[i], n = (int)np_[i], at = (int)sa[i] - 1;
+    if (at < 0 || at >= natom || n <= 0) return false;
+    std::vector<double> a(ex.begin() + off, ex.begin() + off + n), c(cc.begin() + off, cc.begin() + off + n);
+    if (t == -1) {
+      sh.push_back({0, at, a, c});
+      sh.push_back({1, at, a, std::vector<double>(pc.begin() + off, pc.begin() + off + n)});
+    } else {
+      sh.push_back({t, at, a, c});
+    }
+    off += n;
+  }
+  for (const Shell &s : sh)
+    if (std::abs(s.type) > 4) { err = "h primitives not supported in fchk"; return false; }
+  auto nsph = [](int t) { return t < 0 ? 2 * (-t) + 1 : (t + 1) * (t + 2) / 2; };
+  long nb = 0;
+  for (const Shell &s : sh) nb += nsph(s.type);
+  if (nb != nbas) { err = "basis function count does not match the shells"; return false; }
+  // MO coefficients (MO-major, shell order) -> Cartesian components
+  std::vector<const double *> mo(nmoocc);
+  for (int m = 0; m < nmoocc; m++)
+    mo[m] = m < namo ? moa.data() + (size_t)m * nbas : mob.data() + (size_t)(m - namo) * nbas;
+  w = HostWfn();
+  w.natom = (int)natom;
+  w.nmo = nmoocc;
+  w.xyz = xyz;
+  w.z.resize(natom);
+  for (long a = 0; a < natom; a++) w.z[a] = (int)std::lround(zs[a]);
+  std::vector<std::vector<double>> cols;  // per primitive: nmo coefficients
+  long ns = 0;
+  for (const Shell &s : sh) {
+    const int l = std::abs(s.type), ncar = (l + 1) * (l + 2) / 2, nsp = nsph(s.type);
+    const std::vector<int> types = fchk_cart_types(l);
+    const double *T = l == 2 ? &kSphCar2[0][0] : l == 3 ? &kSphCar3[0][0] : l == 4 ? &kSphCar4[0][0] : nullptr;
+    std::vector<double> car((size_t)nmoocc * ncar, 0.0);
+    for (int m = 0; m < nmoocc; m++)
+      for (int c = 0; c < ncar; c++) {
+        if (s.type >= 0 || l < 2) {
+          car[(size_t)m * ncar + c] = mo[m][ns + c];
+        } else {
+          double v = 0.0;
+          for (int k = 0; k < nsp; k++) v += mo[m][ns + k] * T[(size_t)k * ncar + c];
+          car[(size_t)m * ncar + c] = v;
+        }
+      }
+    const int n = (int)s.a.size();
+    for (int c = 0; c < ncar; c++) {
+      const int ityp = types[c];
+      const int *lv = kLi[ityp - 1];
+      std::vector<double> cn(n);
+      for (int k = 0; k < n; k++) cn[k] = s.c[k] * gnorm_cart(lv, s.a[k]);
+      const double norm = aonorm_cart(lv, n, s.a.data(), cn.data());
+      for (int k = 0; k < n; k++) {
+        w.icenter.push_back(s.atom);
+        w.itype.push_back(ityp);
+        w.e.push_back(s.a[k]);
+        std::vector<double> col(nmoocc);
+        for (int m = 0; m < nmoocc; m++) col[m] = cn[k] * norm * car[(size_t)m * ncar + c];
+        cols.push_back(col);
+      }
+    }
+    ns += nsp;
+  }
+  w.npri = (int)w.e.size();
+  w.cmo.resize((size_t)w.npri * nmoocc);
+  for (int i = 0; i < w.npri; i++)
+    std::copy(cols[i].begin(), cols[i].end(), w.cmo.begin() + (size_t)i * nmoocc);
+  w.occ.assign(nmoocc, wfntyp == C2G_WFN_UHF ? 1.0 : 2.0);
+  if (wfntyp == C2G_WFN_ROHF)
+    for (int m = nalf; m < nmoocc; m++) w.occ[m] = 1.0;
+  w.wfntyp = wfntyp;
+  w.nalpha = nalf;
   err.clear();
   prune_primitives(w);
   complete_struct(w);

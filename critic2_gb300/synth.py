@@ -392,3 +392,110 @@ def write_wfn(mol: Molecule, path: str, energies=None) -> None:
     out.append("END DATA")
     with open(path, "w") as fh:
         fh.write("\n".join(out) + "\n")
+
+
+@dataclasses.dataclass
+class ShellBasis:
+    """A contracted-shell basis and MOs as a Gaussian fchk file holds them.
+    shells: (type, atom 0-based, exponents, coefficients, sp p-coefficients
+    or None); type 0 s, 1 p, -1 sp, +-2 d, +-3 f, +-4 g (negative = pure).
+    moa / mob: MO coefficients (nmo, nbas) over the basis functions in
+    shell order."""
+    atom_xyz: np.ndarray
+    atom_z: np.ndarray
+    shells: list
+    nelec: int
+    nalpha: int
+    nbeta: int
+    moa: np.ndarray
+    mob: Optional[np.ndarray] = None
+
+    @property
+    def nbas(self) -> int:
+        return sum(2 * -t + 1 if t < -1 else (4 if t == -1 else (t + 1) * (t + 2) // 2)
+                   for t, *_ in self.shells)
+
+
+def make_shell_basis(seed: int, natom: int = 5, types=(0, -1, 1, -2, 2, -3, 3, -4, 4),
+                     spin: str = "rhf") -> ShellBasis:
+    """Seeded molecule with every shell type on each atom (random exponents
+    and contractions of 1-3 primitives) and random occupied MOs."""
+    rng = np.random.default_rng(seed)
+    box = 4.0 + natom
+    pos = _place_atoms(rng, natom, box, 1)
+    z = rng.choice((1, 6, 7, 8), size=natom).astype(np.int32)
+    shells = []
+    for a in range(natom):
+        for t in types:
+            n = int(rng.integers(1, 4))
+            e = np.sort(np.exp(rng.uniform(np.log(0.2), np.log(30.0), n)))[::-1].copy()
+            c = rng.uniform(0.2, 1.0, n)
+            pc = rng.uniform(0.2, 1.0, n) if t == -1 else None
+            shells.append((t, a, e, c, pc))
+    b = ShellBasis(pos, z, shells, 0, 0, 0, np.zeros((0, 0)))
+    nbas = b.nbas
+    if spin == "rhf":
+        nalpha = nbeta = 6
+    elif spin == "uhf":
+        nalpha, nbeta = 7, 5
+    else:  # rohf
+        nalpha, nbeta = 7, 5
+    b.nelec, b.nalpha, b.nbeta = nalpha + nbeta, nalpha, nbeta
+    nmoa = nbas  # all orbitals, as Gaussian writes them
+    b.moa = rng.standard_normal((nmoa, nbas)) * 0.5
+    if spin == "uhf":
+        b.mob = rng.standard_normal((nmoa, nbas)) * 0.5
+    return b
+
+
+def write_fchk(b: ShellBasis, path: str) -> None:
+    """A Gaussian formatted checkpoint file with the sections read_fchk reads
+    (integers 6 per line in I12, reals 5 per line in E16.8)."""
+    def scalar(name, v):
+        return [f"{name:<40}   I     {v:>12d}"]
+
+    def ints(name, vals):
+        out = [f"{name:<40}   I   N={len(vals):>12d}"]
+        for i in range(0, len(vals), 6):
+            out.append("".join(f"{int(v):12d}" for v in vals[i:i + 6]))
+        return out
+
+    def reals(name, vals):
+        vals = np.ravel(vals)
+        out = [f"{name:<40}   R   N={len(vals):>12d}"]
+        for i in range(0, len(vals), 5):
+            out.append("".join(f"{float(v):16.8E}" for v in vals[i:i + 5]))
+        return out
+
+    nat = len(b.atom_z)
+    ex, cc, pc = [], [], []
+    for t, a, e, c, p in b.shells:
+        ex += list(e)
+        cc += list(c)
+        pc += list(p) if p is not None else [0.0] * len(e)
+    lines = [f"synthetic shell basis", "SP        RHF                                                         Gen"]
+    lines += scalar("Number of atoms", nat)
+    lines += scalar("Charge", 0) + scalar("Multiplicity", 1 + b.nalpha - b.nbeta)
+    lines += scalar("Number of electrons", b.nelec)
+    lines += scalar("Number of alpha electrons", b.nalpha) + scalar("Number of beta electrons", b.nbeta)
+    lines += scalar("Number of basis functions", b.nbas)
+    lines += ints("Atomic numbers", b.atom_z)
+    lines += reals("Current cartesian coordinates", b.atom_xyz)
+    lines += scalar("Number of contracted shells", len(b.shells))
+    lines += scalar("Number of primitive shells", len(ex))
+    lines += scalar("Highest angular momentum", max(abs(s[0]) for s in b.shells))
+    lines += ints("Shell types", [s[0] for s in b.shells])
+    lines += ints("Number of primitives per shell", [len(s[2]) for s in b.shells])
+    lines += ints("Shell to atom map", [s[1] + 1 for s in b.shells])
+    lines += reals("Primitive exponents", ex)
+    lines += reals("Contraction coefficients", cc)
+    if any(s[0] == -1 for s in b.shells):
+        lines += reals("P(S=P) Contraction coefficients", pc)
+    lines += reals("Alpha Orbital Energies", np.linspace(-1, 1, b.moa.shape[0]))
+    if b.mob is not None:
+        lines += reals("Beta Orbital Energies", np.linspace(-1, 1, b.mob.shape[0]))
+    lines += reals("Alpha MO coefficients", b.moa)
+    if b.mob is not None:
+        lines += reals("Beta MO coefficients", b.mob)
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")

@@ -59,6 +59,13 @@ class Wavefunction:
         return cls(_handle=h)
 
     @classmethod
+    def from_fchk(cls, path: str) -> "Wavefunction":
+        """A Gaussian formatted checkpoint file (c2g_wfn_read_fchk)."""
+        h = C.c_void_p()
+        L.check(L.lib().c2g_wfn_read_fchk(path.encode(), C.byref(h)))
+        return cls(_handle=h)
+
+    @classmethod
     def from_wfn(cls, path: str) -> "Wavefunction":
         """An AIMPAC wfn file (c2g_wfn_read_wfn)."""
         h = C.c_void_p()

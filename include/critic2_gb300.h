@@ -96,6 +96,16 @@ int c2g_wfn_read_wfx(const char *path, c2g_wfn **out);
  * src/wfn_private@proc.F90:981-1118. */
 int c2g_wfn_read_wfn(const char *path, c2g_wfn **out);
 
+/* Reads a Gaussian formatted checkpoint (fchk) file's occupied orbitals like
+ * critic2's `load file.fchk`, and creates a handle: sp shells unfolded,
+ * pure d, f and g shells (real solid harmonics, m = 0, 1, -1, 2, -2, ...)
+ * transformed to Cartesian Gaussians, each Cartesian component normalised
+ * by its primitive and contraction factors; RHF, UHF (Beta Orbital
+ * Energies present) or ROHF (alpha and beta counts differ).  h shells are
+ * rejected as in critic2.  Replaces read_fchk without virtual orbitals,
+ * src/wfn_private@proc.F90:1287-1812. */
+int c2g_wfn_read_fchk(const char *path, c2g_wfn **out);
+
 /* Frees the handle and its device memory. */
 int c2g_wfn_destroy(c2g_wfn *h);
 

@@ -521,3 +521,122 @@ def lebedev_rule(n: int) -> np.ndarray:
         with open(os.path.join(here, "..", "tests", "golden", "lebedev_rules.json")) as fh:
             _LEBEDEV = {int(k): np.array(v) for k, v in json.load(fh).items()}
     return _LEBEDEV[n]
+
+
+# ------------------------------------------------------------- fchk format
+_SPHCAR = None
+_FCHK_CART = {0: [""], 1: ["x", "y", "z"], 2: ["xx", "yy", "zz", "xy", "xz", "yz"],
+              3: ["xxx", "yyy", "zzz", "xyy", "xxy", "xxz", "xzz", "yzz", "yyz", "xyz"],
+              4: ["zzzz", "yzzz", "yyzz", "yyyz", "yyyy", "xzzz", "xyzz", "xyyz", "xyyy", "xxzz", "xxyz",
+                  "xxyy", "xxxz", "xxxy", "xxxx"]}
+
+
+def sphcar(l: int) -> np.ndarray:
+    """critic2's spherical -> Cartesian matrix for l (tests/golden/sphcar_fchk.json)."""
+    global _SPHCAR
+    if _SPHCAR is None:
+        import json
+        here = os.path.dirname(os.path.abspath(__file__))
+        with open(os.path.join(here, "..", "tests", "golden", "sphcar_fchk.json")) as fh:
+            _SPHCAR = {int(k): np.array(v) for k, v in json.load(fh).items()}
+    return _SPHCAR[l]
+
+
+def _dfac_l(e):
+    d = 1
+    for v in e:
+        for k in range(2 * v - 1, 1, -2):
+            d *= k
+    return d
+
+
+def _gnorm(e, a):
+    # gnorm (src/wfn_private@proc.F90:3375-3459): 2^((4L+3)/4) a^((2L+3)/4) / pi^(3/4) / sqrt(prod (2l-1)!!)
+    L = sum(e)
+    return 2.0 ** ((4 * L + 3) / 4) * a ** ((2 * L + 3) / 4) / np.pi ** 0.75 / np.sqrt(_dfac_l(e))
+
+
+def _aonorm(e, a, c):
+    # aonorm (:3461-3540)
+    L = sum(e)
+    s = sum(c[i] * c[j] / (a[i] + a[j]) ** (L + 1.5) for i in range(len(a)) for j in range(len(a)))
+    return 1.0 / np.sqrt(s * _dfac_l(e) * np.pi ** 1.5 / 2 ** L)
+
+
+def read_fchk_text(path: str) -> dict:
+    """read_fchk (src/wfn_private@proc.F90:1287-1812, occupied MOs) restated:
+    primitive arrays (icenter 1-based, itype, e, cmo (npri, nmo)), occ,
+    wfntyp, nalpha, atoms; before prune_primitives."""
+    lines = open(path).read().split("\n")
+
+    def scalar(key):
+        for l in lines:
+            if l.startswith(key):
+                return int(l.split()[-1])
+        return 0
+
+    def arr(key, n):
+        for i, l in enumerate(lines):
+            if l.startswith(key):
+                v = []
+                j = i + 1
+                while len(v) < n:
+                    v += [float(t.replace("D", "E")) for t in lines[j].split()]
+                    j += 1
+                return np.array(v[:n])
+        raise KeyError(key)
+
+    nelec, na, nb = scalar("Number of electrons"), scalar("Number of alpha electrons"), scalar("Number of beta electrons")
+    nbas, ncs, nps, nat = (scalar("Number of basis functions"), scalar("Number of contracted shells"),
+                           scalar("Number of primitive shells"), scalar("Atomic numbers"))
+    uhf = any(l.startswith("Beta Orbital Energies") for l in lines)
+    if uhf:
+        typ, nmo, nalf = 1, nelec, na
+    elif na == nb:
+        typ, nmo, nalf = 0, nelec // 2, nelec // 2
+    else:
+        typ, nmo, nalf = 2, na, nb
+    namo = nmo if typ == 2 else nalf
+    st = arr("Shell types", ncs).astype(int)
+    npp = arr("Number of primitives per shell", ncs).astype(int)
+    sa = arr("Shell to atom map", ncs).astype(int)
+    ex, cc = arr("Primitive exponents", nps), arr("Contraction coefficients", nps)
+    pc = arr("P(S=P) Contraction coefficients", nps) if (st == -1).any() else None
+    mo = arr("Alpha MO coefficients", namo * nbas).reshape(namo, nbas)
+    if nmo > namo:
+        mo = np.vstack([mo, arr("Beta MO coefficients", (nmo - namo) * nbas).reshape(nmo - namo, nbas)])
+    shells, off = [], 0
+    for t, n, a in zip(st, npp, sa):
+        e, c = ex[off:off + n], cc[off:off + n]
+        if t == -1:
+            shells += [(0, a, e, c), (1, a, e, pc[off:off + n])]
+        else:
+            shells.append((t, a, e, c))
+        off += n
+    from critic2_gb300.synth import LI
+    li = {tuple(v): k + 1 for k, v in enumerate(LI.tolist())}
+    icenter, itype, pe, cols = [], [], [], []
+    ns = 0
+    for t, a, e, c in shells:
+        l = abs(t)
+        ncar = (l + 1) * (l + 2) // 2
+        nsp = 2 * l + 1 if t < 0 else ncar
+        blk = mo[:, ns:ns + nsp]
+        car = blk @ sphcar(l) if (t < 0 and l >= 2) else blk
+        for k, lab in enumerate(_FCHK_CART[l]):
+            ev = (lab.count("x"), lab.count("y"), lab.count("z"))
+            cn = np.array([ci * _gnorm(ev, ai) for ci, ai in zip(c, e)])
+            norm = _aonorm(ev, e, cn)
+            for j in range(len(e)):
+                icenter.append(a)
+                itype.append(li[ev])
+                pe.append(e[j])
+                cols.append(cn[j] * norm * car[:, k])
+        ns += nsp
+    occ = np.full(nmo, 1.0 if typ == 1 else 2.0)
+    if typ == 2:
+        occ[nalf:] = 1.0
+    return dict(atom_xyz=arr("Current cartesian coordinates", 3 * nat).reshape(nat, 3),
+                atom_z=arr("Atomic numbers", nat).astype(np.int32), icenter=np.array(icenter, np.int32),
+                itype=np.array(itype, np.int32), e=np.array(pe), cmo=np.array(cols), occ=occ, wfntyp=typ,
+                nalpha=nalf)
