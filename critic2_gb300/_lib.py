@@ -18,7 +18,7 @@ PREC = {"fp64": 0, "tf32x3": 1, "bf16x3": 2}
 ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported"}
 
 # every symbol include/critic2_gb300.h declares
-EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx", "c2g_wfn_read_wfn", "c2g_wfn_read_fchk",
+EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx", "c2g_wfn_read_wfn", "c2g_wfn_read_fchk", "c2g_wfn_read_molden",
            "c2g_wfn_destroy", "c2g_wfn_set_edf", "c2g_wfn_set_param", "c2g_wfn_info", "c2g_rho2", "c2g_grd", "c2g_nciplot",
            "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
            "c2g_autocritic", "c2g_nci_post_dev", "c2g_cube_text", "c2g_dat_text", "c2g_nciplot_files",
@@ -81,6 +81,7 @@ def lib():
     L.c2g_wfn_read_wfx.argtypes = [C.c_char_p, C.POINTER(_vp)]
     L.c2g_wfn_read_wfn.argtypes = [C.c_char_p, C.POINTER(_vp)]
     L.c2g_wfn_read_fchk.argtypes = [C.c_char_p, C.POINTER(_vp)]
+    L.c2g_wfn_read_molden.argtypes = [C.c_char_p, C.POINTER(_vp)]
     L.c2g_wfn_destroy.argtypes = [_vp]
     L.c2g_wfn_set_param.argtypes = [_vp, C.c_int, C.c_double]
     L.c2g_wfn_set_edf.argtypes = [_vp, C.c_int, _vp, _vp, _vp, _vp]

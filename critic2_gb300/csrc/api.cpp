@@ -419,6 +419,21 @@ int c2g_wfn_read_wfx(const char *path, c2g_wfn **out) {
   });
 }
 
+int c2g_wfn_read_molden(const char *path, c2g_wfn **out) {
+  return guarded([&] {
+    require(path && out, "null argument");
+    HostWfn w;
+    std::string err;
+    if (!read_molden(path, w, err)) fail(C2G_ERR_IO, err);
+    std::vector<int> icenter1(w.npri);
+    for (int i = 0; i < w.npri; i++) icenter1[i] = w.icenter[i] + 1;
+    int rc = c2g_wfn_create(w.natom, w.xyz.data(), w.z.data(), w.npri, w.nmo, icenter1.data(),
+                            w.itype.data(), w.e.data(), w.occ.data(), w.cmo.data(), w.wfntyp,
+                            w.nalpha, out);
+    if (rc != C2G_OK) fail(rc, g_last_error);
+  });
+}
+
 int c2g_wfn_read_fchk(const char *path, c2g_wfn **out) {
   return guarded([&] {
     require(path && out, "null argument");

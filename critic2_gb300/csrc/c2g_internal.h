@@ -75,6 +75,7 @@ void molecular_cell(HostWfn &w);
 bool read_wfx(const char *path, HostWfn &w, std::string &err);
 bool read_wfn(const char *path, HostWfn &w, std::string &err);
 bool read_fchk(const char *path, HostWfn &w, std::string &err);
+bool read_molden(const char *path, HostWfn &w, std::string &err);
 
 // Cartesian exponents of critic2's li(3,56) table.
 extern const int kLi[56][3];

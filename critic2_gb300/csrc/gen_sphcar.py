@@ -1,8 +1,8 @@
 """Writes sphcar_tables.h: the matrices T(m, c) that take the coefficients
 of normalised real solid harmonic Gaussians (m = 0, 1, -1, 2, -2, ..., the
-order of Gaussian's formatted checkpoint files) to coefficients of
-individually normalised Cartesian Gaussians (fchk's Cartesian order), for
-l = 2, 3, 4.
+order of fchk and molden files) to coefficients of individually
+normalised Cartesian Gaussians (fchk's Cartesian order; for l = 4 also
+molden's), for l = 2, 3, 4.
 
 Derivation (sympy, exact): R_lm = P_l^|m|(z, r) Re/Im[(x + i y)^|m|] with
 P_l^m = sum_k (-1)^k 2^-l C(l,k) C(2l-2k,l) (l-2k)!/(l-2k-m)! r^2k z^(l-2k-m)
@@ -15,6 +15,8 @@ import sympy as sp
 
 x, y, z = sp.symbols("x y z", real=True)
 
+MOLDEN_G = ["xxxx", "yyyy", "zzzz", "xxxy", "xxxz", "xyyy", "yyyz", "xzzz", "yzzz", "xxyy", "xxzz", "yyzz",
+            "xxyz", "xyyz", "xyzz"]
 FCHK_CART = {
     2: ["xx", "yy", "zz", "xy", "xz", "yz"],
     3: ["xxx", "yyy", "zzz", "xyy", "xxy", "xxz", "xzz", "yzz", "yyz", "xyz"],
@@ -56,7 +58,7 @@ def exps(label):
     return (label.count("x"), label.count("y"), label.count("z"))
 
 
-def table(l):
+def table(l, cart=None):
     ms = [0]
     for k in range(1, l + 1):
         ms += [k, -k]
@@ -67,7 +69,7 @@ def table(l):
         n2 = sum(a * b * moment(tuple(p + q for p, q in zip(ea, eb)))
                  for ea, a in coef.items() for eb, b in coef.items())
         row = []
-        for lab in FCHK_CART[l]:
+        for lab in (cart or FCHK_CART[l]):
             e = exps(lab)
             a = coef.get(e, 0)
             row.append(sp.nsimplify(a * sp.sqrt(moment(tuple(2 * v for v in e))) / sp.sqrt(n2)))
@@ -88,6 +90,13 @@ def main():
             out.append("    {" + ", ".join(repr(float(v)) for v in row) + f"}},  // m = {m}")
         out.append("};")
         out.append("")
+    ms, rows = table(4, MOLDEN_G)
+    out.append(f"// l = 4, molden Cartesian order {' '.join(MOLDEN_G)}")
+    out.append("constexpr double kSphCar4Molden[9][15] = {")
+    for m, row in zip(ms, rows):
+        out.append("    {" + ", ".join(repr(float(v)) for v in row) + f"}},  // m = {m}")
+    out.append("};")
+    out.append("")
     out += ["}  // namespace c2g", ""]
     open("sphcar_tables.h", "w").write("\n".join(out))
 

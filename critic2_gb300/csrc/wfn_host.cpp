@@ -720,4 +720,275 @@ bool read_fchk(const char *path, HostWfn &w, std::string &err) {
   return true;
 }
 
+// --------------------------------------------------------------- molden
+namespace {
+
+std::string lower_str(std::string s) {
+  for (char &c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+
+bool parse_real(std::string t, double &v) {
+  for (char &c : t)
+    if (c == 'D' || c == 'd') c = 'E';
+  char *end = nullptr;
+  v = std::strtod(t.c_str(), &end);
+  return end != t.c_str() && *end == '\0';
+}
+
+// molden Cartesian component order of a shell, as critic2 li types
+std::vector<int> molden_cart_types(int l) {
+  if (l != 4) return fchk_cart_types(l);
+  static const char *const g[15] = {"xxxx", "yyyy", "zzzz", "xxxy", "xxxz", "xyyy", "yyyz", "xzzz",
+                                    "yzzz", "xxyy", "xxzz", "yyzz", "xxyz", "xyyz", "xyzz"};
+  std::vector<int> t;
+  for (const char *lab : g) {
+    int e[3] = {0, 0, 0};
+    for (const char *c = lab; *c; c++) e[*c - 'x']++;
+    for (int k = 0; k < 56; k++)
+      if (kLi[k][0] == e[0] && kLi[k][1] == e[1] && kLi[k][2] == e[2]) {
+        t.push_back(k + 1);
+        break;
+      }
+  }
+  return t;
+}
+
+}  // namespace
+
+// read_molden (src/wfn_private@proc.F90:1819-2478) for Gaussian-type
+// orbitals without virtual orbitals: [Atoms] (AU or Angs), [GTO], the
+// [5D]/[5D7F]/[5D10F]/[7F]/[9G] flags, [MO] (occupied MOs, Spin= and
+// Occup=).  ORCA files (title "created by orca_2mkl") are spherical
+// throughout, carry ORCA's primitive normalisation (one factor per l) and
+// the opposite sign of the |m| >= 3 functions.  As in critic2, STO
+// basis sets, sp shells, ROHF and fractional occupations are rejected.
+bool read_molden(const char *path, HostWfn &w, std::string &err) {
+  std::ifstream in(path);
+  if (!in) {
+    err = std::string("cannot open ") + path;
+    return false;
+  }
+  err = std::string("Error reading file: ") + path;
+  std::vector<std::string> lines;
+  for (std::string l; std::getline(in, l);) {
+    if (!l.empty() && l.back() == '\r') l.pop_back();
+    lines.push_back(l);
+  }
+  auto keyword = [&](size_t i) {
+    const std::string l = lower_str(lines[i]);
+    const size_t a = l.find('['), b = l.find(']');
+    return (a == std::string::npos || b == std::string::npos || b < a) ? std::string() : l.substr(a + 1, b - a - 1);
+  };
+  bool is5d = false, is7f = false, is9g = false, isorca = false, gto = false, sto = false;
+  size_t at_line = 0, gto_line = 0, mo_line = 0;
+  double ang = 1.0;
+  for (size_t i = 0; i < lines.size(); i++) {
+    const std::string k = keyword(i);
+    if (k.empty()) continue;
+    if (k == "title" && i + 1 < lines.size() && lines[i + 1].find("created by orca_2mkl") != std::string::npos)
+      isorca = true;
+    else if (k == "atoms") {
+      at_line = i + 1;
+      if (lower_str(lines[i]).find("angs") != std::string::npos) ang = 1.0 / 0.52917720859;
+    } else if (k == "gto") gto = true, gto_line = i + 1;
+    else if (k == "sto") sto = true;
+    else if (k == "mo") mo_line = i + 1;
+    else if (k == "5d" || k == "5d7f") is5d = is7f = true;
+    else if (k == "5d10f") is5d = true, is7f = false;
+    else if (k == "7f") is5d = false, is7f = true;
+    else if (k == "9g") is9g = true;
+  }
+  if (sto) { err = "STO molden files are not supported"; return false; }
+  if (!gto) { err = "No [GTO] or [STO] blocks present"; return false; }
+  if (!at_line || !mo_line) return false;
+  if (isorca) is5d = is7f = is9g = true;
+  // atoms: name index Z x y z
+  std::vector<double> xyz;
+  std::vector<int> zs;
+  for (size_t i = at_line; i < lines.size(); i++) {
+    if (lines[i].find('[') != std::string::npos || trim(lines[i]).empty()) break;
+    std::istringstream ss(lines[i]);
+    std::string name;
+    long idx, z;
+    double v[3];
+    std::string t[3];
+    if (!(ss >> name >> idx >> z >> t[0] >> t[1] >> t[2])) return false;
+    for (int k = 0; k < 3; k++)
+      if (!parse_real(t[k], v[k])) return false;
+    zs.push_back((int)z);
+    for (int k = 0; k < 3; k++) xyz.push_back(v[k] * ang);
+  }
+  const int nat = (int)zs.size();
+  if (nat == 0) { err = "gto found but no atoms"; return false; }
+  // GTO: per atom a header line, then shells "label nprim scale" + primitives, blank line ends the atom
+  struct Shell {
+    int type, atom;
+    std::vector<double> a, c;
+  };
+  std::vector<Shell> sh;
+  size_t i = gto_line;
+  for (int a = 0; a < nat; a++) {
+    while (i < lines.size() && trim(lines[i]).empty()) i++;
+    if (i >= lines.size()) return false;
+    i++;  // atom header
+    while (i < lines.size() && !trim(lines[i]).empty() && lines[i].find('[') == std::string::npos) {
+      std::istringstream ss(lines[i]);
+      std::string lab;
+      long n = 0;
+      if (!(ss >> lab >> n) || n <= 0) { err = "error reading gto block"; return false; }
+      lab = lower_str(lab);
+      int t;
+      if (lab == "s") t = 0;
+      else if (lab == "p") t = 1;
+      else if (lab == "sp") { err = "SP shells are not supported for molden files"; return false; }
+      else if (lab == "d") t = is5d ? -2 : 2;
+      else if (lab == "f") t = is7f ? -3 : 3;
+      else if (lab == "g") t = is9g ? -4 : 4;
+      else { err = "shells above g are not supported for molden files"; return false; }
+      Shell s{t, a, {}, {}};
+      for (long k = 0; k < n; k++) {
+        if (++i >= lines.size()) return false;
+        std::istringstream ps(lines[i]);
+        std::string ta, tc;
+        double va, vc;
+        if (!(ps >> ta >> tc) || !parse_real(ta, va) || !parse_real(tc, vc)) return false;
+        s.a.push_back(va);
+        s.c.push_back(vc);
+      }
+      sh.push_back(s);
+      i++;
+    }
+  }
+  auto nsph = [](int t) { return t < 0 ? 2 * (-t) + 1 : (t + 1) * (t + 2) / 2; };
+  long nbas = 0;
+  for (const Shell &s : sh) nbas += nsph(s.type);
+  // MOs: occupied ones; alpha first, then beta
+  struct MO {
+    bool alpha;
+    int occ;
+    std::vector<double> c;
+  };
+  std::vector<MO> mos;
+  bool alpha = true;
+  for (size_t j = mo_line; j < lines.size(); j++) {
+    const std::string l = lower_str(lines[j]);
+    if (l.find("molden format") != std::string::npos) break;
+    if (l.find('[') != std::string::npos && l.find("[mo]") == std::string::npos && keyword(j) != "") break;
+    if (l.find("spin=") != std::string::npos) alpha = l.find("alpha") != std::string::npos;
+    if (l.find("occup=") == std::string::npos) continue;
+    double o;
+    std::string tok = trim(lines[j].substr(l.find("occup=") + 6));
+    if (!parse_real(tok.substr(0, tok.find_first_of(" \t")), o)) { err = "error reading mo block"; return false; }
+    const long io = std::lround(o);
+    if (std::fabs(o - (double)io) > 1e-6) { err = "Fractional occupations are not supported for molden files"; return false; }
+    if (io != 0 && io != 1 && io != 2) { err = "wrong integer occupation"; return false; }
+    MO m{alpha, (int)io, std::vector<double>(nbas, 0.0)};
+    size_t k = j + 1;
+    for (; k < lines.size(); k++) {
+      std::istringstream ss(lines[k]);
+      std::string ti, tv;
+      if (!(ss >> ti >> tv)) break;
+      char *end = nullptr;
+      const long idx = std::strtol(ti.c_str(), &end, 10);
+      if (end == ti.c_str() || *end != '\0') break;
+      double v;
+      if (!parse_real(tv, v) || idx < 1 || idx > nbas) return false;
+      m.c[idx - 1] = v;
+    }
+    j = k - 1;
+    if (io > 0) mos.push_back(m);
+  }
+  int nelec = 0, nalpha = 0;
+  bool beta = false, had1 = false;
+  for (const MO &m : mos) {
+    nelec += m.occ;
+    nalpha += m.alpha ? 1 : 0;
+    beta = beta || !m.alpha;
+    had1 = had1 || m.occ == 1;
+  }
+  int wfntyp;
+  if (beta) wfntyp = C2G_WFN_UHF;
+  else if (had1) { err = "ROHF wavefunctions are not supported for molden files"; return false; }
+  else wfntyp = C2G_WFN_RHF;
+  if (wfntyp == C2G_WFN_RHF && nelec % 2) { err = "odd nelec but closed-shell wavefunction"; return false; }
+  const int nmo = wfntyp == C2G_WFN_UHF ? nelec : nelec / 2;
+  std::vector<const MO *> ord;
+  for (const MO &m : mos)
+    if (m.alpha) ord.push_back(&m);
+  for (const MO &m : mos)
+    if (!m.alpha) ord.push_back(&m);
+  if ((int)ord.size() != nmo) { err = "inconsistent number of MOs"; return false; }
+  // ORCA's sign convention for |m| >= 3 (f: 6-7, g: 6-9 of the shell)
+  std::vector<std::vector<double>> coef(nmo);
+  for (int m = 0; m < nmo; m++) coef[m] = ord[m]->c;
+  if (isorca) {
+    long ns = 0;
+    for (const Shell &s : sh) {
+      if (s.type == -3 || s.type == -4)
+        for (int m = 0; m < nmo; m++)
+          for (int k = 5; k < (s.type == -3 ? 7 : 9); k++) coef[m][ns + k] = -coef[m][ns + k];
+      ns += nsph(s.type);
+    }
+  }
+  w = HostWfn();
+  w.natom = nat;
+  w.nmo = nmo;
+  w.xyz = xyz;
+  w.z = zs;
+  std::vector<std::vector<double>> cols;
+  long ns = 0;
+  for (const Shell &s : sh) {
+    const int l = std::abs(s.type), ncar = (l + 1) * (l + 2) / 2, nsp = nsph(s.type);
+    const std::vector<int> types = molden_cart_types(l);
+    const double *T = l == 2 ? &kSphCar2[0][0] : l == 3 ? &kSphCar3[0][0] : l == 4 ? &kSphCar4Molden[0][0] : nullptr;
+    std::vector<double> car((size_t)nmo * ncar, 0.0);
+    for (int m = 0; m < nmo; m++)
+      for (int c = 0; c < ncar; c++) {
+        if (s.type >= 0 || l < 2) {
+          car[(size_t)m * ncar + c] = coef[m][ns + c];
+        } else {
+          double v = 0.0;
+          for (int k = 0; k < nsp; k++) v += coef[m][ns + k] * T[(size_t)k * ncar + c];
+          car[(size_t)m * ncar + c] = v;
+        }
+      }
+    const int n = (int)s.a.size();
+    for (int c = 0; c < ncar; c++) {
+      const int ityp = types[c];
+      const int *lv = kLi[ityp - 1];
+      std::vector<double> cn(n);
+      for (int k = 0; k < n; k++) {
+        cn[k] = s.c[k] * gnorm_cart(lv, s.a[k]);
+        if (isorca) {
+          // ORCA normalises every component of a shell like x^l (gnorm_orca)
+          const int xl[3] = {l, 0, 0};
+          cn[k] /= gnorm_cart(xl, s.a[k]);
+        }
+      }
+      const double norm = aonorm_cart(lv, n, s.a.data(), cn.data());
+      for (int k = 0; k < n; k++) {
+        w.icenter.push_back(s.atom);
+        w.itype.push_back(ityp);
+        w.e.push_back(s.a[k]);
+        std::vector<double> col(nmo);
+        for (int m = 0; m < nmo; m++) col[m] = cn[k] * norm * car[(size_t)m * ncar + c];
+        cols.push_back(col);
+      }
+    }
+    ns += nsp;
+  }
+  w.npri = (int)w.e.size();
+  w.cmo.resize((size_t)w.npri * nmo);
+  for (int p = 0; p < w.npri; p++) std::copy(cols[p].begin(), cols[p].end(), w.cmo.begin() + (size_t)p * nmo);
+  w.occ.assign(nmo, wfntyp == C2G_WFN_UHF ? 1.0 : 2.0);
+  w.wfntyp = wfntyp;
+  w.nalpha = nalpha;
+  err.clear();
+  prune_primitives(w);
+  complete_struct(w);
+  molecular_cell(w);
+  return true;
+}
+
 }  // namespace c2g

@@ -499,3 +499,40 @@ def write_fchk(b: ShellBasis, path: str) -> None:
         lines += reals("Beta MO coefficients", b.mob)
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + "\n")
+
+
+def write_molden(b: ShellBasis, path: str, orca: bool = False, angs: bool = False) -> None:
+    """A molden file of the basis (no sp shells; pure or Cartesian per l as
+    the shells say, flagged with [5D7F] / [9G]); occupied MOs only.  With
+    orca=True the title marks an ORCA file."""
+    types = {t for t, *_ in b.shells}
+    assert -1 not in types
+    sym = {1: "H", 6: "C", 7: "N", 8: "O"}
+    out = ["[Molden Format]", "[Title]", " created by orca_2mkl" if orca else " synthetic",
+           "[Atoms] " + ("Angs" if angs else "AU")]
+    f = 0.52917720859 if angs else 1.0
+    for a, (x, zz) in enumerate(zip(b.atom_xyz, b.atom_z)):
+        out.append(f"{sym.get(int(zz), 'X'):>2} {a + 1:5d} {int(zz):4d} " + " ".join(f"{v * f:20.12f}" for v in x))
+    out.append("[GTO]")
+    for a in range(len(b.atom_z)):
+        out.append(f"  {a + 1} 0")
+        for t, at, e, c, _ in b.shells:
+            if at != a:
+                continue
+            out.append(f" {'spdfg'[abs(t)]} {len(e)} 1.00")
+            for ei, ci in zip(e, c):
+                out.append(f"  {ei:20.12E} {ci:20.12E}")
+        out.append("")
+    if -2 in types or -3 in types:
+        out.append("[5D7F]")
+    if -4 in types:
+        out.append("[9G]")
+    out.append("[MO]")
+    spins = [("Alpha", b.moa, b.nalpha)] + ([("Beta", b.mob, b.nbeta)] if b.mob is not None else [])
+    for spin, mo, nocc in spins:
+        for m in range(mo.shape[0]):
+            occ = (2.0 if b.mob is None else 1.0) if m < nocc else 0.0
+            out += [" Sym=     1a", f" Ene= {-1.0 + 0.01 * m:.6f}", f" Spin= {spin}", f" Occup= {occ:.6f}"]
+            out += [f"{k + 1:6d} {v:20.12E}" for k, v in enumerate(mo[m])]
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")

@@ -66,6 +66,13 @@ class Wavefunction:
         return cls(_handle=h)
 
     @classmethod
+    def from_molden(cls, path: str) -> "Wavefunction":
+        """A molden file with Gaussian-type orbitals (c2g_wfn_read_molden)."""
+        h = C.c_void_p()
+        L.check(L.lib().c2g_wfn_read_molden(path.encode(), C.byref(h)))
+        return cls(_handle=h)
+
+    @classmethod
     def from_wfn(cls, path: str) -> "Wavefunction":
         """An AIMPAC wfn file (c2g_wfn_read_wfn)."""
         h = C.c_void_p()

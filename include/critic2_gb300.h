@@ -106,6 +106,15 @@ int c2g_wfn_read_wfn(const char *path, c2g_wfn **out);
  * src/wfn_private@proc.F90:1287-1812. */
 int c2g_wfn_read_fchk(const char *path, c2g_wfn **out);
 
+/* Reads a molden file with Gaussian-type orbitals (occupied MOs; [Atoms]
+ * in AU or Angs, [GTO], [5D]/[5D7F]/[5D10F]/[7F]/[9G], [MO]) like critic2's
+ * `load file.molden`, and creates a handle.  ORCA files (title "created by
+ * orca_2mkl") are spherical throughout, with ORCA's per-l primitive
+ * normalisation and opposite sign of the |m| >= 3 functions.  STO basis
+ * sets, sp shells, ROHF and fractional occupations are rejected, as in
+ * critic2.  Replaces read_molden, src/wfn_private@proc.F90:1819-2478. */
+int c2g_wfn_read_molden(const char *path, c2g_wfn **out);
+
 /* Frees the handle and its device memory. */
 int c2g_wfn_destroy(c2g_wfn *h);
 

@@ -538,7 +538,7 @@ def sphcar(l: int) -> np.ndarray:
         import json
         here = os.path.dirname(os.path.abspath(__file__))
         with open(os.path.join(here, "..", "tests", "golden", "sphcar_fchk.json")) as fh:
-            _SPHCAR = {int(k): np.array(v) for k, v in json.load(fh).items()}
+            _SPHCAR = {(int(k) if k.isdigit() else k): np.array(v) for k, v in json.load(fh).items()}
     return _SPHCAR[l]
 
 
@@ -640,3 +640,120 @@ def read_fchk_text(path: str) -> dict:
                 atom_z=arr("Atomic numbers", nat).astype(np.int32), icenter=np.array(icenter, np.int32),
                 itype=np.array(itype, np.int32), e=np.array(pe), cmo=np.array(cols), occ=occ, wfntyp=typ,
                 nalpha=nalf)
+
+
+_MOLDEN_G = ["xxxx", "yyyy", "zzzz", "xxxy", "xxxz", "xyyy", "yyyz", "xzzz", "yzzz", "xxyy", "xxzz", "yyzz",
+             "xxyz", "xyyz", "xyzz"]
+
+
+def read_molden_text(path: str) -> dict:
+    """read_molden (src/wfn_private@proc.F90:1819-2478; GTO, occupied MOs)
+    restated: primitive arrays as read_fchk_text returns them."""
+    lines = open(path).read().split("\n")
+    low = [l.lower() for l in lines]
+    key = lambda l: l[l.find("[") + 1:l.find("]")] if "[" in l and "]" in l else ""
+    is5d = is7f = is9g = orca = False
+    ang, at, gt, mo0 = 1.0, None, None, None
+    for i, l in enumerate(low):
+        k = key(l)
+        if k == "title" and "created by orca_2mkl" in lines[i + 1]:
+            orca = True
+        elif k == "atoms":
+            at = i + 1
+            if "angs" in l:
+                ang = 1.0 / 0.52917720859
+        elif k == "gto":
+            gt = i + 1
+        elif k == "mo":
+            mo0 = i + 1
+        elif k in ("5d", "5d7f"):
+            is5d = is7f = True
+        elif k == "5d10f":
+            is5d, is7f = True, False
+        elif k == "7f":
+            is5d, is7f = False, True
+        elif k == "9g":
+            is9g = True
+    if orca:
+        is5d = is7f = is9g = True
+    xyz, zs = [], []
+    i = at
+    while lines[i].strip() and "[" not in lines[i]:
+        t = lines[i].split()
+        zs.append(int(t[2]))
+        xyz.append([float(v.replace("D", "E")) * ang for v in t[3:6]])
+        i += 1
+    shells, i = [], gt
+    for a in range(len(zs)):
+        while not lines[i].strip():
+            i += 1
+        i += 1
+        while lines[i].strip() and "[" not in lines[i]:
+            lab, n = lines[i].split()[:2]
+            n = int(n)
+            l = "spdfg".index(lab.lower())
+            pure = {2: is5d, 3: is7f, 4: is9g}.get(l, False)
+            ps = [list(map(lambda v: float(v.replace("D", "E")), lines[i + 1 + k].split()[:2])) for k in range(n)]
+            shells.append((-l if pure else l, a, np.array([p[0] for p in ps]), np.array([p[1] for p in ps])))
+            i += n + 1
+    nbas = sum(2 * -t + 1 if t < 0 else (t + 1) * (t + 2) // 2 for t, *_ in shells)
+    mos, alpha = [], True
+    j = mo0
+    while j < len(lines):
+        l = low[j]
+        if "spin=" in l:
+            alpha = "alpha" in l
+        if "occup=" in l:
+            occ = round(float(l.split("occup=")[1].split()[0]))
+            c = np.zeros(nbas)
+            j += 1
+            while j < len(lines):
+                t = lines[j].split()
+                if len(t) < 2 or not t[0].lstrip("-").isdigit():
+                    break
+                c[int(t[0]) - 1] = float(t[1].replace("D", "E"))
+                j += 1
+            if occ > 0:
+                mos.append((alpha, occ, c))
+            continue
+        j += 1
+    beta = any(not a for a, _, _ in mos)
+    typ = 1 if beta else 0
+    mo = np.array([c for a, _, c in mos if a] + [c for a, _, c in mos if not a])
+    nalf = sum(1 for a, _, _ in mos if a)
+    if orca:
+        ns = 0
+        for t, *_ in shells:
+            if t in (-3, -4):
+                mo[:, ns + 5:ns + (7 if t == -3 else 9)] *= -1
+            ns += 2 * -t + 1 if t < 0 else (t + 1) * (t + 2) // 2
+    from critic2_gb300.synth import LI
+    li = {tuple(v): k + 1 for k, v in enumerate(LI.tolist())}
+    icenter, itype, pe, cols = [], [], [], []
+    ns = 0
+    for t, a, e, c in shells:
+        l = abs(t)
+        cart = _MOLDEN_G if l == 4 else _FCHK_CART[l]
+        ncar = len(cart)
+        nsp = 2 * l + 1 if t < 0 else ncar
+        blk = mo[:, ns:ns + nsp]
+        if t < 0 and l >= 2:
+            blk = blk @ (sphcar(l) if l < 4 else _sphcar_molden_g())
+        for k, lab in enumerate(cart):
+            ev = (lab.count("x"), lab.count("y"), lab.count("z"))
+            cn = np.array([ci * _gnorm(ev, ai) / (_gnorm((l, 0, 0), ai) if orca else 1.0) for ci, ai in zip(c, e)])
+            norm = _aonorm(ev, e, cn)
+            for jj in range(len(e)):
+                icenter.append(a + 1)
+                itype.append(li[ev])
+                pe.append(e[jj])
+                cols.append(cn[jj] * norm * blk[:, k])
+        ns += nsp
+    return dict(atom_xyz=np.array(xyz), atom_z=np.array(zs, np.int32), icenter=np.array(icenter, np.int32),
+                itype=np.array(itype, np.int32), e=np.array(pe), cmo=np.array(cols),
+                occ=np.full(mo.shape[0], 1.0 if typ == 1 else 2.0), wfntyp=typ, nalpha=nalf)
+
+
+def _sphcar_molden_g():
+    sphcar(2)  # loads the fixture
+    return _SPHCAR["4molden"]

@@ -1,5 +1,6 @@
 """Writes sphcar_fchk.json: critic2's spherical -> Cartesian matrices used by
-read_fchk (dsphcar, fsphcar, gsphcar_fchk; src/wfn_private@proc.F90:46-167),
+read_fchk and read_molden (dsphcar, fsphcar, gsphcar_fchk, gsphcar;
+src/wfn_private@proc.F90:46-167),
 parsed from the reference source with its named sqrt constants resolved,
 as T[m][c] (m = 0, 1, -1, ...; Cartesian components in fchk order).
 Run in the build container (it reads the reference tree):
@@ -33,7 +34,8 @@ def value(tok):
 
 
 out = {}
-for name, key, nm, nc in (("dsphcar", "2", 5, 6), ("fsphcar", "3", 7, 10), ("gsphcar_fchk", "4", 9, 15)):
+for name, key, nm, nc in (("dsphcar", "2", 5, 6), ("fsphcar", "3", 7, 10), ("gsphcar_fchk", "4", 9, 15),
+                          ("gsphcar", "4molden", 9, 15)):
     body = src.split(f"real*8 :: {name}({nm},{nc}) = reshape((/&")[1].split("/),shape")[0]
     nums = []
     for line in body.split("\n"):

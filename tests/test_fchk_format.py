@@ -20,10 +20,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def test_derived_matrices_equal_critic2s():
     gold = json.load(open(os.path.join(ROOT, "tests", "golden", "sphcar_fchk.json")))
     text = open(os.path.join(ROOT, "critic2_gb300", "csrc", "sphcar_tables.h")).read()
-    for l in (2, 3, 4):
-        body = text.split(f"kSphCar{l}[")[1].split("};")[0]
+    for name, key in (("kSphCar2[", "2"), ("kSphCar3[", "3"), ("kSphCar4[", "4"), ("kSphCar4Molden[", "4molden")):
+        body = text.split(name)[1].split("};")[0]
         T = np.array([[float(v) for v in r.split(",")] for r in re.findall(r"\{([^{}]+)\}", body)])
-        assert np.array_equal(T, np.array(gold[str(l)])), l
+        assert np.array_equal(T, np.array(gold[key])), key
 
 
 def dfm1(n):
