@@ -9,13 +9,19 @@
 //   N = (component, point) pairs of a 32-point tile (B = the basis block chi
 //       built in shared memory, one row per component and point),
 //   K = one 32-byte row of primitives (16 bf16 or 8 tf32),
-// in a 3-product split: A_hi*B_hi + A_hi*B_lo + A_lo*B_hi, FP32 accumulate;
-// per K-step six MMAs: hi*hi of components 0-7 (N = 256) and 8-9 (N = 64),
-// the two cross products of the value and gradient (N = 128, own
-// accumulator) and of the second derivatives (N = 192, into the main
-// accumulator).  The accumulators (320 columns for the hi*hi products, 128
-// for the cross products of the value and gradient) and 4 coefficient
-// stages (16 columns each) fill the SM's 512 TMEM columns.
+// in a 3-product split: A_hi*B_hi + A_hi*B_lo + A_lo*B_hi, FP32 accumulate.
+// The tensor core's FP32 accumulation rounds toward zero, so every MMA into
+// an accumulator shrinks it by up to an ulp of its size; the value
+// component (the density) is protected from that bias: its hi*hi products
+// rotate over four accumulators (K-step j into accumulator j mod 4) and its
+// cross products have their own.  Per K-step eight or nine MMAs: hi*hi of
+// components 0-7 (N = 256) or of component 0 alone (N = 32, accumulators
+// 1-3) plus 1-7 (N = 224), hi*hi of 8-9 (N = 64), the two cross products
+// of the value (N = 32) and those of components 1-9 (N = 128 + 160, into
+// the main accumulator).  The accumulators (320 columns for the hi*hi
+// products, 96 for three more value accumulators, 32 for the value's cross
+// products) and 4 coefficient stages (16 columns each) fill the SM's 512
+// TMEM columns.
 //
 // CTA roles (persistent, one CTA per SM, 12 warps):
 //   warps 0-3  load the coefficient stage (L2 -> registers -> tcgen05.st into
@@ -112,17 +118,16 @@ constexpr int W_MMA = 4, W_SETUP = 5, W_PROD0 = 6;
 constexpr int NTHR = (W_PROD0 + NPROD) * 32;  // 384
 constexpr uint32_t TMEM_COLS = 512;
 // TMEM columns: the accumulators of the hi*hi products of the 10 components
-// (320 columns, column = component * 32 + point), the accumulators of the
-// cross products (hi*lo + lo*hi) of the value and the gradient (128
-// columns), then the coefficient buffers.  Keeping the small cross terms
-// apart means the large accumulator takes one truncating addition per MMA
-// step instead of three (the tensor core's FP32 accumulation rounds toward
-// zero, so the error grows with the number of additions); the cross terms
-// of the second derivatives go into the main accumulator.
-constexpr int NXCOMP = 4;
-constexpr int XROWS = NXCOMP * NP;          // 128
-constexpr int XCOL0 = BROWS;                // 320
-constexpr int CBUF0 = XCOL0 + XROWS;        // 448
+// (320 columns, column = component * 32 + point), three more accumulators
+// of the value's hi*hi products (96 columns), the accumulator of the value's
+// cross products (hi*lo + lo*hi, 32 columns), then the coefficient buffers.
+// Each value accumulator takes one truncating addition every fourth K-step,
+// at a quarter of the size; the cross terms of the derivatives go into the
+// main accumulator.
+constexpr int NVACC = 4;                    // value accumulators
+constexpr int DV0 = BROWS;                  // 320: value accumulators 1-3
+constexpr int XCOL0 = DV0 + (NVACC - 1) * NP;  // 416: the value's cross products
+constexpr int CBUF0 = XCOL0 + NP;           // 448
 static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
 constexpr int TAB = 4 * 13;  // axis-factor table: 4 primitives x (1 x + 4 y + 8 z values)
@@ -252,6 +257,40 @@ __device__ __forceinline__ bool thread_wait(const Smem &s, int bar, uint32_t par
   return true;
 }
 
+// 2^r for |r| <= 1/2 (+ a few ulp): 1 + r q(r) with q of degree 6, a
+// weighted least-squares fit of (2^r - 1)/r on 400 Chebyshev nodes of
+// [-0.501, 0.501] (relative error 2.7e-9 in exact arithmetic, FP32
+// coefficients; gen_exp2.py); Horner in FP32 and a final fma keep the
+// result within one ulp.
+__device__ __forceinline__ float exp2_poly(float r) {
+  float q = 1.51654758155928e-05f;
+  q = fmaf(q, r, 1.546717103337869e-04f);
+  q = fmaf(q, r, 1.3334084069356322e-03f);
+  q = fmaf(q, r, 9.618036448955536e-03f);
+  q = fmaf(q, r, 5.5504102259874344e-02f);
+  q = fmaf(q, r, 2.4022650718688965e-01f);
+  q = fmaf(q, r, 6.931471824645996e-01f);
+  return fmaf(q, r, 1.f);
+}
+
+// 2^(xh + xl) for |xh| < 126, xl a correction below ulp(xh): n = rint(xh),
+// 2^n by the exponent field, 2^((xh - n) + xl) by exp2_poly (xh - n is
+// exact).  Within one ulp over the range; FP32's own exp2f is within two,
+// and the rounding of a product argument alone (xl = 0) costs up to
+// |x| * 2^-24 * ln 2 relative.
+__device__ __forceinline__ float exp2_ff(float xh, float xl) {
+  const float n = rintf(xh);
+  const float p = exp2_poly((xh - n) + xl);
+  const int ni = max(-126, min(127, (int)n));
+  return __int_as_float(__float_as_int(p) + ni * 8388608);
+}
+
+// exp2(-(a * t)) with the rounding error of the product carried along
+__device__ __forceinline__ float exp2_neg_prod(float a, float t) {
+  const float xh = -a * t;
+  return exp2_ff(xh, fmaf(-a, t, -xh));
+}
+
 // Factors of one Cartesian axis (see k_fp64.cu): with t = -2 alpha,
 //   f0 = x^l, f1 = l x^(l-1) + t x^(l+1), f2 = l(l-1) x^(l-2) + t(2l+1) x^l + t^2 x^(l+2)
 // Generic form (any l), used for stages that hold g or h functions.
@@ -315,7 +354,7 @@ __device__ __forceinline__ StagePrim stage_prim(const PrimTC &pr, const float4 &
   const float f = (u - n) + ue;
   const float on = sqrtf(ooh);
   q.direct = pr.alpha * (2.f * on * rad + rad * rad) > 60.f;
-  q.g = q.direct ? 1.f : ((n > 250.f) ? 0.f : ldexpf(exp2f(-f), -(int)n));
+  q.g = q.direct ? 1.f : ((n > 250.f) ? 0.f : ldexpf(exp2_poly(-f), -(int)n));
   // cutoff threshold on t (factorised) or on |d|^2 (direct); -inf for padding
   q.t = pr.dran > 0.f ? (q.direct ? pr.dran * pr.dran : pr.dran * pr.dran - (ooh + ool)) : -INFINITY;
   q.al2e = pr.al2e;
@@ -364,7 +403,7 @@ __device__ __forceinline__ void chi10(const StagePrim &q, const PointD &d, float
   const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
   const float targ = q.direct ? d2 : t;
   const bool in = d.valid && (targ <= q.t);
-  const float e = exp2f(-q.al2e * targ);
+  const float e = exp2_neg_prod(q.al2e, targ);
   const float ex = in ? q.g * e : 0.f;
   const float tt = -2.f * q.alpha;
   float x0, x1, x2, y0, y1, y2, z0, z1, z2;
@@ -491,7 +530,7 @@ __device__ __noinline__ void produce_half_brick(const StageRow *rows, int half, 
         const float4 o = rows[j].o, l = rows[j].l, c = rows[j].c;
         const float targ = (X.w + Y.w) + Z.w;
         const bool in = d.valid && (targ <= l.w);
-        const float ex = in ? o.w * exp2f(-c.x * targ) : 0.f;
+        const float ex = in ? o.w * exp2_neg_prod(c.x, targ) : 0.f;
         const float yz = Y.x * Z.x * ex, xz = X.x * Z.x * ex, xy = X.x * Y.x * ex;
         cc[q][0] = X.x * yz;
         cc[q][1] = X.y * yz;
@@ -876,9 +915,15 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
     if (lane == 0) {
       constexpr uint32_t fmt = KIND == 0 ? 1 : 2;
       constexpr uint32_t id_256 = ptx::make_idesc(fmt, K::MT, 256);  // components 0-7
+      constexpr uint32_t id_224 = ptx::make_idesc(fmt, K::MT, 224);  // components 1-7
+      constexpr uint32_t id_160 = ptx::make_idesc(fmt, K::MT, 160);  // components 5-9
+      constexpr uint32_t id_128 = ptx::make_idesc(fmt, K::MT, 128);  // components 1-4
       constexpr uint32_t id_64 = ptx::make_idesc(fmt, K::MT, 64);    // components 8-9
-      constexpr uint32_t id_x = ptx::make_idesc(fmt, K::MT, K::XROWS);            // components 0-3
-      constexpr uint32_t id_h = ptx::make_idesc(fmt, K::MT, K::BROWS - K::XROWS);  // components 4-9
+      constexpr uint32_t id_32 = ptx::make_idesc(fmt, K::MT, 32);    // component 0
+      auto mma = [](uint32_t d, uint32_t a_t, uint64_t b_d, uint32_t id, uint32_t acc) {
+        if constexpr (KIND == 0) ptx::mma_bf16_ts(d, a_t, b_d, id, acc);
+        else ptx::mma_tf32_ts(d, a_t, b_d, id, acc);
+      };
       uint32_t g = 0, u = 0;
       bool ok = true;
       for (int t = 0; t < ntl && ok; t++) {
@@ -901,29 +946,33 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
             {
               const uint32_t sh = sb, sl = sb + K::BPIECE;
               const uint32_t dcol = tmem, xcol = tmem + K::XCOL0;
+              // B row r of the 320-row piece starts r / 8 row groups of 256
+              // bytes in: rows 0, 32 (component 1), 160 (5), 256 (8)
               const uint64_t bh = ptx::smem_desc_kmajor(sh, 128, 256);
               const uint64_t bl = ptx::smem_desc_kmajor(sl, 128, 256);
-              // rows 256-319 (components 8-9) start 32 row groups in, rows
-              // 128-319 (components 4-9) 16 row groups in
+              const uint64_t bh1 = ptx::smem_desc_kmajor(sh + 4 * 256, 128, 256);
+              const uint64_t bl1 = ptx::smem_desc_kmajor(sl + 4 * 256, 128, 256);
+              const uint64_t bh5 = ptx::smem_desc_kmajor(sh + 20 * 256, 128, 256);
+              const uint64_t bl5 = ptx::smem_desc_kmajor(sl + 20 * 256, 128, 256);
               const uint64_t bh8 = ptx::smem_desc_kmajor(sh + 32 * 256, 128, 256);
-              const uint64_t bh4 = ptx::smem_desc_kmajor(sh + 16 * 256, 128, 256);
-              const uint64_t bl4 = ptx::smem_desc_kmajor(sl + 16 * 256, 128, 256);
-              const uint32_t d8 = dcol + 256, d4 = dcol + K::XROWS;
-              if constexpr (KIND == 0) {
-                ptx::mma_bf16_ts(dcol, a_hi, bh, id_256, acc0);
-                ptx::mma_bf16_ts(d8, a_hi, bh8, id_64, acc0);
-                ptx::mma_bf16_ts(xcol, a_hi, bl, id_x, acc0);
-                ptx::mma_bf16_ts(xcol, a_lo, bh, id_x, 1u);
-                ptx::mma_bf16_ts(d4, a_hi, bl4, id_h, 1u);
-                ptx::mma_bf16_ts(d4, a_lo, bh4, id_h, 1u);
+              // hi*hi: the value of K-step j goes to value accumulator j mod 4
+              // (0 = the main one, whose first write initialises components 0-7)
+              const int va = j % K::NVACC;
+              if (va == 0) {
+                mma(dcol, a_hi, bh, id_256, acc0);
               } else {
-                ptx::mma_tf32_ts(dcol, a_hi, bh, id_256, acc0);
-                ptx::mma_tf32_ts(d8, a_hi, bh8, id_64, acc0);
-                ptx::mma_tf32_ts(xcol, a_hi, bl, id_x, acc0);
-                ptx::mma_tf32_ts(xcol, a_lo, bh, id_x, 1u);
-                ptx::mma_tf32_ts(d4, a_hi, bl4, id_h, 1u);
-                ptx::mma_tf32_ts(d4, a_lo, bh4, id_h, 1u);
+                mma(tmem + K::DV0 + (va - 1) * K::NP, a_hi, bh, id_32, j >= K::NVACC ? 1u : 0u);
+                mma(dcol + 32, a_hi, bh1, id_224, 1u);
               }
+              mma(dcol + 256, a_hi, bh8, id_64, acc0);
+              // cross products: the value's apart, components 1-9 into the
+              // main accumulator (initialised above in the first K-step)
+              mma(xcol, a_hi, bl, id_32, acc0);
+              mma(xcol, a_lo, bh, id_32, 1u);
+              mma(dcol + 32, a_hi, bl1, id_128, 1u);
+              mma(dcol + 160, a_hi, bl5, id_160, 1u);
+              mma(dcol + 32, a_lo, bh1, id_128, 1u);
+              mma(dcol + 160, a_lo, bh5, id_160, 1u);
             }
             ptx::mma_commit(&s.bar[K::B_EMPTY + b]);
           }
@@ -1017,21 +1066,29 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           const float occ = a.occ[mo];
 #pragma unroll 1
           for (int ch = 0; ch < 4; ch++) {
-            uint32_t v[10][8], xv[K::NXCOMP][8];
+            uint32_t v[10][8], xv[8], dv[K::NVACC - 1][8];
             // points ch*8 .. ch*8+7
             const uint32_t dc = tmem + lanebase + ch * 8;
             const uint32_t xc = tmem + lanebase + K::XCOL0 + ch * 8;
 #pragma unroll
             for (int c = 0; c < 10; c++) ptx::tmem_ld8(dc + c * K::NP, v[c]);
 #pragma unroll
-            for (int c = 0; c < K::NXCOMP; c++) ptx::tmem_ld8(xc + c * K::NP, xv[c]);
+            ptx::tmem_ld8(xc, xv);
+            // value accumulator c + 1 holds K-steps c + 1, c + 5, ...: written iff nact > c + 1
+#pragma unroll
+            for (int c = 0; c < K::NVACC - 1; c++) {
+#pragma unroll
+              for (int i = 0; i < 8; i++) dv[c][i] = 0u;
+              if (nact > c + 1) ptx::tmem_ld8(tmem + lanebase + K::DV0 + c * K::NP + ch * 8, dv[c]);
+            }
             ptx::tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-              const float p0 = __uint_as_float(v[0][j]) + __uint_as_float(xv[0][j]);
-              const float px = __uint_as_float(v[1][j]) + __uint_as_float(xv[1][j]);
-              const float py = __uint_as_float(v[2][j]) + __uint_as_float(xv[2][j]);
-              const float pz = __uint_as_float(v[3][j]) + __uint_as_float(xv[3][j]);
+              const float p0 = ((__uint_as_float(v[0][j]) + __uint_as_float(dv[0][j])) +
+                                (__uint_as_float(dv[1][j]) + __uint_as_float(dv[2][j]))) + __uint_as_float(xv[j]);
+              const float px = __uint_as_float(v[1][j]);
+              const float py = __uint_as_float(v[2][j]);
+              const float pz = __uint_as_float(v[3][j]);
               const float o2 = 2.f * occ, t0 = o2 * p0;
               const float ux = o2 * px, uy = o2 * py, uz = o2 * pz;
               float *rw = red + lane * K::RED + j;
