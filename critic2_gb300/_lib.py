@@ -19,7 +19,7 @@ ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported"}
 
 # every symbol include/critic2_gb300.h declares
 EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx", "c2g_wfn_read_wfn", "c2g_wfn_read_fchk", "c2g_wfn_read_molden",
-           "c2g_wfn_destroy", "c2g_wfn_set_edf", "c2g_wfn_set_param", "c2g_wfn_info", "c2g_rho2", "c2g_grd", "c2g_nciplot",
+           "c2g_wfn_destroy", "c2g_wfn_set_edf", "c2g_wfn_set_param", "c2g_wfn_info", "c2g_rho2", "c2g_rho2_valence", "c2g_grd", "c2g_nciplot",
            "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
            "c2g_autocritic", "c2g_nci_post_dev", "c2g_cube_text", "c2g_dat_text", "c2g_nciplot_files",
            "c2g_grid_field_dev", "c2g_cube_precise_text", "c2g_cube_field_file",
@@ -93,6 +93,7 @@ def lib():
     L.c2g_nci_chk_read.argtypes = [C.c_char_p, _dp, _dp, _ip, _dp, _dp, C.POINTER(C.c_int)]
     L.c2g_wfn_info.argtypes = [_vp] + [C.POINTER(C.c_int)] * 5
     L.c2g_rho2.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int] + [_vp] * 6
+    L.c2g_rho2_valence.argtypes = [_vp, C.c_int, _vp, C.c_int] + [_vp] * 3
     L.c2g_grd.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int] + [_vp] * 8
     L.c2g_nciplot.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, C.POINTER(NciStats)]
     L.c2g_nciplot_dev.argtypes = [_vp, _dp, _dp, _ip, C.c_int, _vp, _vp, _vp, C.POINTER(NciStats)]

@@ -180,11 +180,14 @@ int check_prec(int prec) {
 }
 
 // Evaluates the FP64 record (kRecFull when full) at n host points.
-std::vector<double> eval_records_fp64(Handle &h, int n, const double *xyz, int nder, bool full) {
+std::vector<double> eval_records_fp64(Handle &h, int n, const double *xyz, int nder, bool full,
+                                      bool valence = false) {
   const int nr = full ? kRecFull : kRecNci;
   DevBuf dx(sizeof(double) * 3 * (size_t)n), dr(sizeof(double) * nr * (size_t)n);
   C2G_CUDA(cudaMemcpy(dx.p, xyz, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice));
-  launch_fp64_points(h.dev, n, dx.as<double>(), nder, full, dr.as<double>(), 0);
+  DevWfn dw = h.dev;
+  if (valence) dw.nedf = 0;  // the EDF core left out: rho2's rhoval/gradval/hval
+  launch_fp64_points(dw, n, dx.as<double>(), nder, full, dr.as<double>(), 0);
   std::vector<double> rec((size_t)nr * n);
   C2G_CUDA(cudaMemcpy(rec.data(), dr.p, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost));
   return rec;
@@ -528,6 +531,21 @@ int c2g_rho2(c2g_wfn *hp, int n, const double *xyz, int nder, int prec, double *
                     grad ? grad + 9 * i : nullptr, hess ? hess + 27 * i : nullptr,
                     gkin ? gkin + 3 * i : nullptr, stress ? stress + 9 * i : nullptr,
                     vir ? vir + i : nullptr);
+  });
+}
+
+int c2g_rho2_valence(c2g_wfn *hp, int n, const double *xyz, int nder, double *rho, double *grad, double *hess) {
+  return guarded([&] {
+    Handle *h = check_handle(hp);
+    require(n >= 0, "negative point count");
+    require(nder >= 0 && nder <= 2, "nder must be 0, 1 or 2");
+    if (n == 0) return;
+    require(xyz != nullptr, "null xyz");
+    DeviceGuard g(h->device);
+    std::vector<double> rec = eval_records_fp64(*h, n, xyz, nder, true, true);
+    for (int i = 0; i < n; i++)
+      assemble_rho2(h->host, rec.data() + (size_t)i * kRecFull, nder, rho ? rho + 3 * i : nullptr,
+                    grad ? grad + 9 * i : nullptr, hess ? hess + 27 * i : nullptr, nullptr, nullptr, nullptr);
   });
 }
 

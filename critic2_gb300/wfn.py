@@ -129,6 +129,17 @@ class Wavefunction:
                                  L.ptr(out["stress"]), L.ptr(out["vir"])))
         return out
 
+    def rho2_valence(self, xyz, nder: int = 2) -> dict:
+        """The valence outputs of molwfn%rho2 (rhoval, gradval, hval: no
+        EDF core), FP64, in rho2's layout: rho (n,3), grad (n,3,3), hess
+        (n,3,3,3)."""
+        x = _f64(xyz).reshape(-1, 3)
+        n = x.shape[0]
+        out = dict(rho=np.zeros((n, 3)), grad=np.zeros((n, 3, 3)), hess=np.zeros((n, 3, 3, 3)))
+        L.check(L.lib().c2g_rho2_valence(self._h, n, L.ptr(x), nder, L.ptr(out["rho"]),
+                                         L.ptr(out["grad"]), L.ptr(out["hess"])))
+        return out
+
     def grd(self, xyz, nder: int = 2, prec="fp64") -> dict:
         """field%grd at points xyz (n,3): f, gf (n,3), gfmod, hf (n,3,3),
         hfeval (n,3) ascending, r, s, isnuc."""

@@ -170,6 +170,13 @@ int c2g_wfn_info(const c2g_wfn *h, int *natom, int *npri, int *nmo, int *wfntyp,
 int c2g_rho2(c2g_wfn *h, int n, const double *xyz, int nder, int prec, double *rho,
              double *grad, double *hess, double *gkin, double *stress, double *vir);
 
+/* The valence outputs of molwfn%rho2 (rhoval, gradval, hval: the density
+ * without the EDF core, src/wfn_private@proc.F90:2484-2705), FP64, in the
+ * layout of c2g_rho2's rho, grad and hess (any may be NULL).  Equal to
+ * c2g_rho2's for a wavefunction without EDF primitives. */
+int c2g_rho2_valence(c2g_wfn *h, int n, const double *xyz, int nder, double *rho, double *grad,
+                     double *hess);
+
 /* field%grd for the wavefunction field at n points: molecular-cell wrap,
  * rho2, nucleus check (|grad| := 0 within 1e-5 bohr of a nucleus),
  * Hessian eigenvalues (ascending), rank r and signature s with the 1e-8

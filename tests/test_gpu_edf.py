@@ -173,3 +173,24 @@ def test_set_edf_rejects_bad_input(gpu_lib, mol_edf):
         g.set_edf([1], [57], [1.0], [1.0])
     with pytest.raises(_lib.C2GError):
         g.set_edf([1], [1], [-1.0], [1.0])
+
+
+@pytest.mark.parametrize("wfntyp", [0, 1])
+def test_rho2_valence_leaves_the_core_out(gpu_lib, oracle_mod, mol_edf, wfntyp):
+    """c2g_rho2_valence against rho2's rhoval/gradval/hval in the oracle, and
+    equal to the full evaluation of the same MOs without EDF primitives."""
+    from critic2_gb300.wfn import Wavefunction
+    m = mol_edf if wfntyp == 0 else spin_variant(mol_edf, wfntyp)
+    bare = dataclasses.replace(m, edf_icenter=None, edf_itype=None, edf_e=None, edf_c=None)
+    g = Wavefunction(m)
+    pts = near_points(m, 48, 11 + wfntyp)
+    v = g.rho2_valence(pts, 2)
+    full = g.rho2(pts, 2, "fp64")
+    o = oracle_mod.Wfn(m)
+    for i in range(0, len(pts), 4):
+        r = o.grd(pts[i], 2)
+        assert close([v["rho"][i, 0]], [r.fval])
+        assert abs(np.trace(v["hess"][i, 0]) - r.del2fval) <= 1e-10 * max(abs(r.del2fval), abs(r.fval))
+    assert np.median(full["rho"][:, 0] - v["rho"][:, 0]) > 0  # the core adds density near the nuclei
+    vb = Wavefunction(bare).rho2(pts, 2, "fp64")
+    assert close(v["rho"], vb["rho"]) and close(v["grad"], vb["grad"]) and close(v["hess"], vb["hess"])
