@@ -247,6 +247,32 @@ __device__ __forceinline__ bool warp_wait(const Smem &s, int bar, uint32_t parit
   return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
+// A producer's wait for its stage buffer, taken just before the first
+// store into the buffer, so that the part of the basis block computed in
+// registers overlaps the MMAs that still read the buffer.
+struct BufWait {
+  uint64_t *bar;
+  volatile int *abort;
+  int *err;
+  uint32_t parity;
+  int bit;
+  bool need;
+};
+
+__device__ __forceinline__ bool buf_wait(const BufWait &w) {
+  if (!w.need) return true;
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    if (*w.abort) ok = 0;
+    else if (!ptx::mbar_wait(w.bar, w.parity, K::TIMEOUT_NS)) {
+      ok = 0;
+      *w.abort = 1;
+      atomicOr(w.err, w.bit);
+    }
+  }
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
 __device__ __forceinline__ bool thread_wait(const Smem &s, int bar, uint32_t parity, int *err) {
   if (*s.abort) return false;
   if (!ptx::mbar_wait(&s.bar[bar], parity, K::TIMEOUT_NS)) {
@@ -442,7 +468,8 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
 // matrices of 16 bytes; the two K-halves 128 bytes apart, 8-row groups 256
 // bytes apart).
 template <int KIND, bool ANYL>
-__device__ __noinline__ void produce_half(const StageRow *rows, int half, const PointD &d, uint8_t *dst) {
+__device__ __noinline__ bool produce_half(const StageRow *rows, int half, const PointD &d, uint8_t *dst,
+                                          BufWait bw) {
   constexpr int PPB = KIND == 0 ? 8 : 4;  // primitives per 16-byte half row
   const int r = threadIdx.x & 31;
   uint32_t wv[10][2][4];
@@ -473,6 +500,7 @@ __device__ __noinline__ void produce_half(const StageRow *rows, int half, const 
   }
   // B row of component c at point r = c * 32 + r, whose 8-row group is
   // 4c + (r >> 3)
+  if (!buf_wait(bw)) return false;
   uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
 #pragma unroll
   for (int c = 0; c < 10; c++)
@@ -480,6 +508,7 @@ __device__ __noinline__ void produce_half(const StageRow *rows, int half, const 
     for (int pc = 0; pc < 2; pc++)
       *reinterpret_cast<uint4 *>(row + pc * K::BPIECE + c * 1024) =
           make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
+  return true;
 }
 
 // Brick form of produce_half: per group of 4 primitives, the warp first
@@ -488,8 +517,8 @@ __device__ __noinline__ void produce_half(const StageRow *rows, int half, const 
 // offsets, then every lane forms chi from the three entries of its point.
 // The factors and the per-primitive data are the ones of chi10.
 template <int KIND, bool ANYL>
-__device__ __noinline__ void produce_half_brick(const StageRow *rows, int half, const PointD &d, uint8_t *dst,
-                                                float4 *tab, const float4 *dlt) {
+__device__ __noinline__ bool produce_half_brick(const StageRow *rows, int half, const PointD &d, uint8_t *dst,
+                                                float4 *tab, const float4 *dlt, BufWait bw) {
   constexpr int PPB = KIND == 0 ? 8 : 4;
   const int r = threadIdx.x & 31;
   const int jo = r >> 3, ko = r & 7;
@@ -564,6 +593,7 @@ __device__ __noinline__ void produce_half_brick(const StageRow *rows, int half, 
       }
     }
   }
+  if (!buf_wait(bw)) return false;
   uint8_t *row = dst + (r >> 3) * 256 + half * 128 + (r & 7) * 16;
 #pragma unroll
   for (int c = 0; c < 10; c++)
@@ -571,13 +601,14 @@ __device__ __noinline__ void produce_half_brick(const StageRow *rows, int half, 
     for (int pc = 0; pc < 2; pc++)
       *reinterpret_cast<uint4 *>(row + pc * K::BPIECE + c * 1024) =
           make_uint4(wv[c][pc][0], wv[c][pc][1], wv[c][pc][2], wv[c][pc][3]);
+  return true;
 }
 
 // Builds one K-stage of the basis block (lane = point row).  The stage's
 // primitive data is loaded once (lane j holds primitive j) and broadcast.
 template <int KIND>
-__device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
-                                        const PointD &d, float rad, StageRow *rows, float4 *tab) {
+__device__ __forceinline__ bool produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
+                                        const PointD &d, float rad, StageRow *rows, float4 *tab, BufWait bw) {
   constexpr int KPS = KIND == 0 ? 16 : 8;
   const int r = threadIdx.x & 31;
   int lmax = 0;
@@ -591,19 +622,22 @@ __device__ __forceinline__ void produce(const TcArgs &a, const Smem &s, int par,
     lmax = max(q.lp & 15, max((q.lp >> 4) & 15, (q.lp >> 8) & 15));
   }
   lmax = __reduce_max_sync(0xffffffffu, lmax);  // also orders the row writes before the reads
+  // the buffer wait is taken inside the first half, before its stores
+  bool ok = true;
   if (s.brick[par]) {
     const float4 *dlt = s.dl + par * 32;
-    for (int half = 0; half < 2; half++) {
-      if (lmax <= 3) produce_half_brick<KIND, false>(rows, half, d, dst, tab, dlt);
-      else produce_half_brick<KIND, true>(rows, half, d, dst, tab, dlt);
+    for (int half = 0; half < 2 && ok; half++, bw.need = false) {
+      if (lmax <= 3) ok = produce_half_brick<KIND, false>(rows, half, d, dst, tab, dlt, bw);
+      else ok = produce_half_brick<KIND, true>(rows, half, d, dst, tab, dlt, bw);
     }
   } else {
-    for (int half = 0; half < 2; half++) {
-      if (lmax <= 3) produce_half<KIND, false>(rows, half, d, dst);
-      else produce_half<KIND, true>(rows, half, d, dst);
+    for (int half = 0; half < 2 && ok; half++, bw.need = false) {
+      if (lmax <= 3) ok = produce_half<KIND, false>(rows, half, d, dst, bw);
+      else ok = produce_half<KIND, true>(rows, half, d, dst, bw);
     }
   }
   __syncwarp();
+  return ok;
 }
 
 // per-point outputs -----------------------------------------------------------
@@ -1007,10 +1041,12 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           if ((int)(g % K::NPROD) != pw) continue;
           const int sk = list[j];
           const int b = g % K::NSTAGE;
-          if (g >= (uint32_t)K::NSTAGE && !(ok = warp_wait(s, K::B_EMPTY + b, ((g / K::NSTAGE) - 1) & 1, a.err)))
+          const int eb = K::B_EMPTY + b;
+          const BufWait bw{&s.bar[eb], s.abort, a.err, ((g / K::NSTAGE) - 1) & 1u, 1 << (eb < 31 ? eb : 31),
+                           g >= (uint32_t)K::NSTAGE};
+          if (!(ok = produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, rad, s.rows + pw * 16,
+                                   s.tab + pw * K::TAB, bw)))
             break;
-          produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, rad, s.rows + pw * 16,
-                        s.tab + pw * K::TAB);
           ptx::fence_proxy_async_smem();
           __syncwarp();
           if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_CHI + b]);
