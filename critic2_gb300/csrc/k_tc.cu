@@ -26,15 +26,17 @@
 // CTA roles (persistent, one CTA per SM, 12 warps):
 //   warps 0-3  load the coefficient stage (L2 -> registers -> tcgen05.st into
 //              TMEM) and run the epilogue: tcgen05.ld of phi, the
-//              occupation-weighted products, the MO reduction (cross-lane via
-//              shared memory), FP64 accumulation over MO tiles, and the NCI
-//              or record output;
+//              occupation-weighted products and the MO reduction (cross-lane
+//              via shared memory) into per-quadrant partial sums;
 //   warp 4     allocates TMEM; lane 0 issues the MMAs and commits;
 //   warp 5     prepares each point tile: coordinates, per-atom offsets and
 //              the list of K-stages that any point of the tile can see (a
 //              stage is skipped only when every (point, primitive) pair in it
 //              is beyond critic2's cutoff, so skipping changes no result),
-//              ordered from the least to the most important one;
+//              ordered from the least to the most important one; after the
+//              next tile's setup it runs the previous tile's sink: the sum
+//              of the partial sums, FP64 accumulation over MO tiles, and the
+//              NCI or record output;
 //   warps 6-11 build the basis block chi (value, gradient, Hessian of every
 //              primitive at the 32 points, split hi/lo) for one K-stage each.
 // Hand-offs use mbarriers; tcgen05.commit releases shared stages and
@@ -843,6 +845,41 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
   const int ntl = ntiles > (int)blockIdx.x ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
 
   if (warp == K::W_SETUP) {
+    // The sink of a tile (sum of the four quadrants' partial sums, FP64
+    // accumulation over MO tiles, the NCI or record output) runs here, after
+    // the next tile's setup, so that its FP64 work stays off the loader /
+    // epilogue warps that feed the next tile's MMAs.  One lane per point.
+    auto sink_tile = [&](int tt) -> bool {
+      const int pp = tt & 1;
+      const int p = lane;
+      for (int mt = 0; mt < a.nmt; mt++) {
+        const uint32_t uu = (uint32_t)tt * (uint32_t)a.nmt + (uint32_t)mt;
+        if (!warp_wait(s, K::B_EPIFULL, uu & 1, a.err)) return false;
+        float v4[10];
+#pragma unroll
+        for (int k = 0; k < 10; k++) {
+          const int i = (p >> 3) * 80 + k * 8 + (p & 7);
+          v4[k] = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
+        }
+        const long idx = s.idx[pp * 32 + p];
+        const double *xp = s.x + (pp * 32 + p) * 3;
+        if (a.nmt == 1) {
+          if (idx >= 0) put_point(a, sink, idx, v4, 1, xp);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 10; k++) s.acc[k * 32 + p] += (double)v4[k];
+          if (mt == a.nmt - 1) {
+            if (idx >= 0) put_point(a, sink, idx, s.acc + p, 32, xp);
+#pragma unroll
+            for (int k = 0; k < 10; k++) s.acc[k * 32 + p] = 0.0;
+          }
+        }
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_EPIFREE]);
+      }
+      return true;
+    };
+    bool sink_ok = true;
     // ---------------------------------------------------------- tile setup
     for (int t = 0; t < ntl; t++) {
       const int par = t & 1;
@@ -943,7 +980,9 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       }
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_TREADY + par]);
+      if (t >= 1 && !(sink_ok = sink_tile(t - 1))) break;
     }
+    if (sink_ok && ntl > 0) sink_tile(ntl - 1);
   } else if (warp == K::W_MMA) {
     // ------------------------------------------------------------ MMA issue
     if (lane == 0) {
@@ -1096,7 +1135,8 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
         // ----- epilogue of this (point tile, MO tile)
         if (!(ok = warp_wait(s, K::B_ACCFULL, u & 1, a.err))) break;
         ptx::tc_fence_after();
-        if (q != 0 && u > 0 && !(ok = warp_wait(s, K::B_EPIFREE, (u - 1) & 1, a.err))) break;
+        // s.part is read by the setup warp's sink of the previous (tile, MO tile)
+        if (u > 0 && !(ok = warp_wait(s, K::B_EPIFREE, (u - 1) & 1, a.err))) break;
         float *part = s.part + q * 320;
         if (nact > 0) {
           const float occ = a.occ[mo];
@@ -1157,31 +1197,6 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
         if (lane == 0) {
           ptx::mbar_arrive(&s.bar[K::B_ACCEMPTY]);
           ptx::mbar_arrive(&s.bar[K::B_EPIFULL]);
-        }
-        if (q == 0) {
-          if (!(ok = warp_wait(s, K::B_EPIFULL, u & 1, a.err))) break;
-          const int p = lane;
-          float v4[10];
-#pragma unroll
-          for (int k = 0; k < 10; k++) {
-            const int i = (p >> 3) * 80 + k * 8 + (p & 7);
-            v4[k] = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
-          }
-          const long idx = s.idx[par * 32 + p];
-          const double *xp = s.x + (par * 32 + p) * 3;
-          if (a.nmt == 1) {
-            if (idx >= 0) put_point(a, sink, idx, v4, 1, xp);
-          } else {
-#pragma unroll
-            for (int k = 0; k < 10; k++) s.acc[k * 32 + p] += (double)v4[k];
-            if (mt == a.nmt - 1) {
-              if (idx >= 0) put_point(a, sink, idx, s.acc + p, 32, xp);
-#pragma unroll
-              for (int k = 0; k < 10; k++) s.acc[k * 32 + p] = 0.0;
-            }
-          }
-          __syncwarp();
-          if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_EPIFREE]);
         }
       }
       __syncwarp();
