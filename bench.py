@@ -44,9 +44,9 @@ from critic2_gb300 import synth  # noqa: E402
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 # DRAM bytes (read + write) per grid point of the split evaluator, from one
-# ncu capture of k_tc on the nci60 molecule with a 64^3 grid (1.04 MB per
+# ncu capture of k_tc on the nci60 molecule with a 64^3 grid (1.09 MB per
 # 262,144 points; traffic grows with the points, the operands stay in L2).
-TRAFFIC_PER_POINT = {("nci60", "tf32x3"): (1.035776e6 + 0.0) / 262144}
+TRAFFIC_PER_POINT = {("nci60", "tf32x3"): (1.087232e6 + 5.12e3) / 262144}
 
 
 def env_int(k, d):
