@@ -207,3 +207,20 @@ def test_nci60_density_error_distribution(gpu_lib):
     assert abs(np.mean((r32 - r64) / r64)) <= 1.5e-7
     assert np.abs(s32 - s64).max() <= 1e-3
     assert np.array_equal(np.sign(c32), np.sign(c64))
+
+
+def test_nci_grid_multi_mo_tile(gpu_lib):
+    """NCI grid of a molecule with 200 MOs (two 128-MO tiles): the tile sink
+    accumulates the MO tiles in FP64 before the NCI output.  TF32x3 against
+    the GPU's FP64 plain form on a 40^3 grid through the molecule's centre."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("cp100")
+    w = Wavefunction(mol)
+    x0, xm, ns = synth.nci_grid(mol, 40, 0.15)
+    c64, s64, _ = w.nciplot(x0, xm, ns, "fp64")
+    c, s, st = w.nciplot(x0, xm, ns, "tf32x3")
+    rho64, rho = np.abs(c64) / 100, np.abs(c) / 100
+    assert st.npoints == c.size
+    assert rel(rho, rho64, 1e-300) < TOL["tf32x3"]["rho"]
+    assert np.max(np.abs(s - s64)) < TOL["tf32x3"]["s"]
+    assert int((np.sign(c) != np.sign(c64)).sum()) <= 2
