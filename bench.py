@@ -48,6 +48,10 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # 262,144 points; traffic grows with the points, the operands stay in L2).
 TRAFFIC_PER_POINT = {("nci60", "tf32x3"): (1.087232e6 + 5.12e3) / 262144}
 
+# Dense TF32 tensor rate of this GPU model, measured with a cuBLAS TF32 GEMM
+# on the same GPUs (TFLOP/s); the driver's peaks file holds BF16 only.
+TF32_MEASURED_TFLOPS = 1006.0
+
 
 def env_int(k, d):
     try:
@@ -392,7 +396,16 @@ def main():
                          "traffic": (TRAFFIC_PER_POINT[(args.workload, prec)] * npts
                                      if (args.workload, prec) in TRAFFIC_PER_POINT else None),
                          "note": f"algorithmic 20*nmo*npri flops per point over the evaluation "
-                                 f"kernel time; peak = bf16 dense burst ({pk_kind})"},
+                                 f"kernel time; peak = bf16 dense burst ({pk_kind})",
+                         # the split products issue three MMAs per multiply (hi*hi, hi*lo, lo*hi)
+                         "issued": None if prec == "fp64" else {
+                             "achieved": 3 * achieved,
+                             "peak": peak if prec == "bf16x3" else TF32_MEASURED_TFLOPS,
+                             "frac": 3 * achieved / (peak if prec == "bf16x3" else TF32_MEASURED_TFLOPS),
+                             "note": "3x the algorithmic rate (three products per split multiply); "
+                                     "dense count, so K-stages skipped by the cutoffs count as work and "
+                                     "frac can exceed 1; peak = " + ("bf16 dense burst" if prec == "bf16x3"
+                                                                     else "tf32 dense, cuBLAS-measured")}},
             "fp64_recheck_points": nrecheck}
     if fp64:
         line["fp64_plain"] = fp64
