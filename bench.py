@@ -321,6 +321,7 @@ def main():
     torch.cuda.synchronize()
     ms_kernel = st.ms_kernel
     nrecheck = int(st.nrecheck)
+    stage_frac = float(st.stage_frac)  # K-stages a 32-point tile computes, of all
     # end-to-end through the public call with host output arrays
     e2e_ms = []
     for _ in range(max(1, min(args.steps, 3))):
@@ -402,9 +403,15 @@ def main():
                              "achieved": 3 * achieved,
                              "peak": peak if prec == "bf16x3" else TF32_MEASURED_TFLOPS,
                              "frac": 3 * achieved / (peak if prec == "bf16x3" else TF32_MEASURED_TFLOPS),
+                             "stage_frac": stage_frac,
+                             "effective_achieved": 3 * achieved * stage_frac,
+                             "effective_frac": 3 * achieved * stage_frac /
+                                               (peak if prec == "bf16x3" else TF32_MEASURED_TFLOPS),
                              "note": "3x the algorithmic rate (three products per split multiply); "
                                      "dense count, so K-stages skipped by the cutoffs count as work and "
-                                     "frac can exceed 1; peak = " + ("bf16 dense burst" if prec == "bf16x3"
+                                     "frac can exceed 1; effective_* scales it by the fraction of "
+                                     "K-stages the tiles compute (MO and stage padding not counted); "
+                                     "peak = " + ("bf16 dense burst" if prec == "bf16x3"
                                                                      else "tf32 dense, cuBLAS-measured")}},
             "fp64_recheck_points": nrecheck}
     if fp64:
