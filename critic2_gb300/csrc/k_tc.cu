@@ -137,6 +137,10 @@ constexpr uint64_t TIMEOUT_NS = 4000000000ull;
 // barrier slots
 constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17, B_EPIFULL = 18,
               B_EPIFREE = 19, B_TREADY = 20, B_TFREE = 22, B_DRAIN = 24, NBAR = 25;
+// One producer warp per stage buffer.  The buffer waits are mbarrier parity
+// waits; with more producers than buffers the producer of stage g could wait
+// for stage g - NSTAGE while stage g - 2 NSTAGE still holds the buffer, and
+// the parity would alias.
 static_assert(NSTAGE == NPROD, "one producer warp per stage buffer");
 }  // namespace K
 
