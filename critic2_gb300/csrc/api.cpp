@@ -495,6 +495,9 @@ int c2g_wfn_set_param(c2g_wfn *hp, int param, double value) {
     } else if (param == C2G_PARAM_NEWTON_STALL) {
       require(value >= 0.0 && value <= 1e6, "stall count must be in [0, 1e6]");
       h->newton_stall = (int)value;
+    } else if (param == C2G_PARAM_WAIT_NS) {
+      require(value >= 1.0 && value <= 6e11, "wait limit must be in [1, 6e11] ns");
+      tc_set_wait_ns(*h, (uint64_t)value);
     } else {
       fail(C2G_ERR_ARG, "unknown parameter");
     }

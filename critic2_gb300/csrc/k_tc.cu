@@ -40,8 +40,9 @@
 //   warps 6-11 build the basis block chi (value, gradient, Hessian of every
 //              primitive at the 32 points, split hi/lo) for one K-stage each.
 // Hand-offs use mbarriers; tcgen05.commit releases shared stages and
-// signals the accumulators.  Every wait is bounded: on a timeout the CTA sets
-// an error flag, stops, drains its MMAs and frees TMEM.
+// signals the accumulators.  Every wait is bounded (TcArgs::wait_ns, the
+// handle's C2G_PARAM_WAIT_NS): on a timeout the CTA sets an error flag,
+// stops, drains its MMAs and frees TMEM.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -98,7 +99,10 @@ struct TcOperands {
   std::vector<int> order;  // TC primitive order (indices into the handle's prims)
   std::vector<void *> allocs;
   double recheck_rel = -1.0;  // < 0: the mode's default (TF32x3 1e-4, BF16x3 1e-3)
+  uint64_t wait_ns = 4000000000ull;  // limit of every pipeline wait of the split kernel
   int *scratch = nullptr;  // re-check list + counter, grown on demand
+  uint8_t *atab = nullptr;  // per-CTA atom tables when they do not fit shared memory
+  size_t atab_cap = 0;      // bytes
   size_t scratch_cap = 0;  // ints
 };
 
@@ -133,7 +137,6 @@ constexpr int CBUF0 = XCOL0 + NP;           // 448
 static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
 constexpr int TAB = 4 * 13;  // axis-factor table: 4 primitives x (1 x + 4 y + 8 z values)
-constexpr uint64_t TIMEOUT_NS = 4000000000ull;
 // barrier slots
 constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17, B_EPIFULL = 18,
               B_EPIFREE = 19, B_TREADY = 20, B_TFREE = 22, B_DRAIN = 24, NBAR = 25;
@@ -161,9 +164,13 @@ struct TcArgs {
   int recheck_cap;
   float recheck_rel;
   unsigned long long *stage_count;  // total active (tile, stage) pairs, or null
+  uint64_t wait_ns;                 // limit of every pipeline wait
+  uint8_t *atab;                    // per-CTA atom tables in global memory, or null (shared memory)
+  size_t atab_stride;               // bytes per CTA
 };
 
 struct Smem {
+  uint64_t wait_ns;  // limit of every pipeline wait (TcArgs::wait_ns)
   uint8_t *stage;
   float *red, *part;
   double *acc;
@@ -181,11 +188,17 @@ struct Smem {
   float4 *offl;  // [2][natom] (o - o_hi, |o|^2 - |o|^2_hi)
   float *dmin;   // [2][natom] lower bound of the tile-atom distance
   StageRow *rows;  // [NPROD][16] stage primitive data of each producer warp
+  double4 *rowsd;  // [NPROD][16] centre and FP64 exponent of the same primitives (point-list tiles)
   float4 *tab;     // [NPROD][52] axis-factor tables of the brick path
   int *brick;      // [2] tile is a separable brick (see the setup warp)
 };
 
-__host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs) {
+// Bytes of the per-tile atom tables (off, offl, dmin for two tiles).
+__host__ __device__ inline size_t atom_table_bytes(int natom) { return ((size_t)2 * natom * 36 + 15) / 16 * 16; }
+
+// Shared-memory layout; the atom tables (offs[10-12]) are in it when
+// atoms_smem, else in a per-CTA slice of global memory.
+__host__ __device__ inline size_t smem_bytes(int natom, int maskw, bool atoms_smem, size_t *offs) {
   size_t o = 0;
   auto take = [&](size_t n, size_t al) {
     o = (o + al - 1) / al * al;
@@ -203,18 +216,20 @@ __host__ __device__ inline size_t smem_bytes(int natom, int maskw, size_t *offs)
   offs[7] = take(K::NBAR * 8, 16);
   offs[8] = take(64, 16);
   offs[9] = take((size_t)2 * maskw * 32 * 3, 16);  // key (1 B) + list (2 B) per stage
-  offs[10] = take((size_t)2 * natom * 16, 16);
-  offs[11] = take((size_t)2 * natom * 16, 16);
-  offs[12] = take((size_t)2 * natom * 4, 16);
-  offs[13] = take((size_t)K::NPROD * 16 * sizeof(StageRow), 16);
+  offs[13] = take((size_t)K::NPROD * 16 * (sizeof(StageRow) + sizeof(double4)), 16);
   offs[14] = take((size_t)K::NPROD * K::TAB * sizeof(float4), 16);
+  const size_t at = atoms_smem ? take(atom_table_bytes(natom), 16) : 0;
+  offs[10] = at;
+  offs[11] = at + (size_t)2 * natom * 16;
+  offs[12] = at + (size_t)4 * natom * 16;
   return o + 1024;  // slack for aligning the dynamic base
 }
 
-__device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
+__device__ inline Smem carve(uint8_t *raw, const TcArgs &a) {
+  const int natom = a.w.natom, maskw = a.maskw;
   uint8_t *base = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
   size_t o[15];
-  smem_bytes(natom, maskw, o);
+  smem_bytes(natom, maskw, a.atab == nullptr, o);
   Smem s;
   s.stage = base + o[0];
   s.red = (float *)(base + o[1]);
@@ -230,12 +245,16 @@ __device__ inline Smem carve(uint8_t *raw, int natom, int maskw) {
   s.rad = (float *)(base + o[8] + 16);
   s.key = (uint8_t *)(base + o[9]);
   s.list = (uint16_t *)(base + o[9] + (size_t)2 * maskw * 32);
-  s.off = (float4 *)(base + o[10]);
-  s.offl = (float4 *)(base + o[11]);
-  s.dmin = (float *)(base + o[12]);
+  // the atom tables: in shared memory, or in this CTA's slice of a.atab
+  uint8_t *ab = a.atab ? a.atab + (size_t)blockIdx.x * a.atab_stride - o[10] : base;
+  s.off = (float4 *)(ab + o[10]);
+  s.offl = (float4 *)(ab + o[11]);
+  s.dmin = (float *)(ab + o[12]);
   s.rows = (StageRow *)(base + o[13]);
+  s.rowsd = (double4 *)(base + o[13] + (size_t)K::NPROD * 16 * sizeof(StageRow));
   s.tab = (float4 *)(base + o[14]);
   s.brick = (int *)(base + o[8] + 24);
+  s.wait_ns = a.wait_ns;
   return s;
 }
 
@@ -244,7 +263,7 @@ __device__ __forceinline__ bool warp_wait(const Smem &s, int bar, uint32_t parit
   int ok = 1;
   if ((threadIdx.x & 31) == 0) {
     if (*s.abort) ok = 0;
-    else if (!ptx::mbar_wait(&s.bar[bar], parity, K::TIMEOUT_NS)) {
+    else if (!ptx::mbar_wait(&s.bar[bar], parity, s.wait_ns)) {
       ok = 0;
       *s.abort = 1;
       atomicOr(err, 1 << (bar < 31 ? bar : 31));
@@ -260,6 +279,7 @@ struct BufWait {
   uint64_t *bar;
   volatile int *abort;
   int *err;
+  uint64_t wait_ns;
   uint32_t parity;
   int bit;
   bool need;
@@ -270,7 +290,7 @@ __device__ __forceinline__ bool buf_wait(const BufWait &w) {
   int ok = 1;
   if ((threadIdx.x & 31) == 0) {
     if (*w.abort) ok = 0;
-    else if (!ptx::mbar_wait(w.bar, w.parity, K::TIMEOUT_NS)) {
+    else if (!ptx::mbar_wait(w.bar, w.parity, w.wait_ns)) {
       ok = 0;
       *w.abort = 1;
       atomicOr(w.err, w.bit);
@@ -281,7 +301,7 @@ __device__ __forceinline__ bool buf_wait(const BufWait &w) {
 
 __device__ __forceinline__ bool thread_wait(const Smem &s, int bar, uint32_t parity, int *err) {
   if (*s.abort) return false;
-  if (!ptx::mbar_wait(&s.bar[bar], parity, K::TIMEOUT_NS)) {
+  if (!ptx::mbar_wait(&s.bar[bar], parity, s.wait_ns)) {
     *s.abort = 1;
     atomicOr(err, 1 << (bar < 31 ? bar : 31));
     return false;
@@ -421,9 +441,11 @@ __device__ __forceinline__ StagePrim bcast(const StagePrim &v, int j) {
   return q;
 }
 
-// Point data: delta (offset from the tile reference), 2*delta, |delta|^2.
+// Point data: delta (offset from the tile reference), 2*delta, |delta|^2,
+// and the point itself (FP64, for the point-list path).
 struct PointD {
   float x, y, z, x2, y2, z2, dd;
+  double px, py, pz;
   bool valid;
 };
 
@@ -462,10 +484,67 @@ __device__ __forceinline__ void chi10(const StagePrim &q, const PointD &d, float
   chi[9] = y1 * z1 * x0 * ex;
 }
 
+// chi (10 components) of one primitive at one point, with the Gaussian's
+// argument alpha |x - A|^2 formed in FP64 from the point and the centre A =
+// (ax, ay, az, alpha in FP64) and passed to exp2 as a float-float: the form
+// of point lists (c2g_rho2, c2g_grd, meshes, Newton seeds), whose 32-point
+// tiles can span several bohr, where the tile-factorised Gaussian of chi10
+// would carry the FP32 rounding of a large per-point argument.  Zero beyond
+// the cutoff (|x - A|^2 <= dran2).
+template <bool ANYL>
+__device__ __forceinline__ void chi10_exact(const StagePrim &q, const double4 &A, float dran2, const PointD &d,
+                                            float (&chi)[10]) {
+  const double ddx = d.px - A.x, ddy = d.py - A.y, ddz = d.pz - A.z;
+  const double d2 = fma(ddx, ddx, fma(ddy, ddy, ddz * ddz));
+  const bool in = d.valid && (d2 <= (double)dran2);
+  const double xd = -(A.w * d2) * 1.4426950408889634;
+  const float xh = (float)xd;
+  const float ex = in ? exp2_ff(xh, (float)(xd - (double)xh)) : 0.f;
+  const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+  const float tt = -2.f * q.alpha;
+  float x0, x1, x2, y0, y1, y2, z0, z1, z2;
+  if constexpr (ANYL) {
+    axis_any(dx, q.lp & 15, tt, x0, x1, x2);
+    axis_any(dy, (q.lp >> 4) & 15, tt, y0, y1, y2);
+    axis_any(dz, (q.lp >> 8) & 15, tt, z0, z1, z2);
+  } else {
+    axis_f(dx, q.lp & 15, tt, x0, x1, x2);
+    axis_f(dy, (q.lp >> 4) & 15, tt, y0, y1, y2);
+    axis_f(dz, (q.lp >> 8) & 15, tt, z0, z1, z2);
+  }
+  const float yz = y0 * z0 * ex, xz = x0 * z0 * ex, xy = x0 * y0 * ex;
+  chi[0] = x0 * yz;
+  chi[1] = x1 * yz;
+  chi[2] = y1 * xz;
+  chi[3] = z1 * xy;
+  chi[4] = x2 * yz;
+  chi[5] = y2 * xz;
+  chi[6] = z2 * xy;
+  const float x1e = x1 * ex;
+  chi[7] = x1e * y1 * z0;
+  chi[8] = x1e * z1 * y0;
+  chi[9] = y1 * z1 * x0 * ex;
+}
+
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return r;
+}
+
+// chi = x0 + x1: TF32 pieces, each rounded to nearest.
+__device__ __forceinline__ void split_tf32(float v, uint32_t &x0, uint32_t &x1) {
+  x0 = tf32_rna(v);
+  x1 = tf32_rna(v - __uint_as_float(x0));
+}
+
+// The same for a pair of values as BF16x2 words.
+__device__ __forceinline__ void split_bf16(float a, float b, uint32_t &x0, uint32_t &x1) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  x0 = *reinterpret_cast<const uint32_t *>(&h);
+  x1 = *reinterpret_cast<const uint32_t *>(&l);
 }
 
 // One 16-byte half of the 32-byte K-row of one point: PPB primitives,
@@ -474,7 +553,7 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
 // matrices of 16 bytes; the two K-halves 128 bytes apart, 8-row groups 256
 // bytes apart).
 template <int KIND, bool ANYL>
-__device__ __noinline__ bool produce_half(const StageRow *rows, int half, const PointD &d, uint8_t *dst,
+__device__ __noinline__ bool produce_half(const StageRow *rows, const double4 *rowsd, int half, const PointD &d, uint8_t *dst,
                                           BufWait bw) {
   constexpr int PPB = KIND == 0 ? 8 : 4;  // primitives per 16-byte half row
   const int r = threadIdx.x & 31;
@@ -483,25 +562,16 @@ __device__ __noinline__ bool produce_half(const StageRow *rows, int half, const 
   for (int j = 0; j < PPB; j += (KIND == 0 ? 2 : 1)) {
     if constexpr (KIND == 0) {
       float c0[10], c1[10];
-      chi10<ANYL>(load_stage_prim(rows, half * PPB + j), d, c0);
-      chi10<ANYL>(load_stage_prim(rows, half * PPB + j + 1), d, c1);
+      chi10_exact<ANYL>(load_stage_prim(rows, half * PPB + j), rowsd[half * PPB + j], rows[half * PPB + j].l.w, d, c0);
+      chi10_exact<ANYL>(load_stage_prim(rows, half * PPB + j + 1), rowsd[half * PPB + j + 1],
+                        rows[half * PPB + j + 1].l.w, d, c1);
 #pragma unroll
-      for (int c = 0; c < 10; c++) {
-        const __nv_bfloat162 hi = __floats2bfloat162_rn(c0[c], c1[c]);
-        const float2 hf = __bfloat1622float2(hi);
-        const __nv_bfloat162 lo = __floats2bfloat162_rn(c0[c] - hf.x, c1[c] - hf.y);
-        wv[c][0][j >> 1] = *reinterpret_cast<const uint32_t *>(&hi);
-        wv[c][1][j >> 1] = *reinterpret_cast<const uint32_t *>(&lo);
-      }
+      for (int c = 0; c < 10; c++) split_bf16(c0[c], c1[c], wv[c][0][j >> 1], wv[c][1][j >> 1]);
     } else {
       float c0[10];
-      chi10<ANYL>(load_stage_prim(rows, half * PPB + j), d, c0);
+      chi10_exact<ANYL>(load_stage_prim(rows, half * PPB + j), rowsd[half * PPB + j], rows[half * PPB + j].l.w, d, c0);
 #pragma unroll
-      for (int c = 0; c < 10; c++) {
-        const uint32_t hi = tf32_rna(c0[c]);
-        wv[c][0][j] = hi;
-        wv[c][1][j] = tf32_rna(c0[c] - __uint_as_float(hi));
-      }
+      for (int c = 0; c < 10; c++) split_tf32(c0[c], wv[c][0][j], wv[c][1][j]);
     }
   }
   // B row of component c at point r = c * 32 + r, whose 8-row group is
@@ -582,20 +652,10 @@ __device__ __noinline__ bool produce_half_brick(const StageRow *rows, int half, 
       const int wd = (g0 + jp) >> (KIND == 0 ? 1 : 0);
       if constexpr (KIND == 0) {
 #pragma unroll
-        for (int c = 0; c < 10; c++) {
-          const __nv_bfloat162 hi = __floats2bfloat162_rn(cc[0][c], cc[1][c]);
-          const float2 hf = __bfloat1622float2(hi);
-          const __nv_bfloat162 lo = __floats2bfloat162_rn(cc[0][c] - hf.x, cc[1][c] - hf.y);
-          wv[c][0][wd] = *reinterpret_cast<const uint32_t *>(&hi);
-          wv[c][1][wd] = *reinterpret_cast<const uint32_t *>(&lo);
-        }
+        for (int c = 0; c < 10; c++) split_bf16(cc[0][c], cc[1][c], wv[c][0][wd], wv[c][1][wd]);
       } else {
 #pragma unroll
-        for (int c = 0; c < 10; c++) {
-          const uint32_t hi = tf32_rna(cc[0][c]);
-          wv[c][0][wd] = hi;
-          wv[c][1][wd] = tf32_rna(cc[0][c] - __uint_as_float(hi));
-        }
+        for (int c = 0; c < 10; c++) split_tf32(cc[0][c], wv[c][0][wd], wv[c][1][wd]);
       }
     }
   }
@@ -614,23 +674,30 @@ __device__ __noinline__ bool produce_half_brick(const StageRow *rows, int half, 
 // primitive data is loaded once (lane j holds primitive j) and broadcast.
 template <int KIND>
 __device__ __forceinline__ bool produce(const TcArgs &a, const Smem &s, int par, int stage_k, uint8_t *dst,
-                                        const PointD &d, float rad, StageRow *rows, float4 *tab, BufWait bw) {
+                                        const PointD &d, float rad, StageRow *rows, double4 *rowsd, float4 *tab,
+                                        BufWait bw) {
   constexpr int KPS = KIND == 0 ? 16 : 8;
   const int r = threadIdx.x & 31;
+  const bool brick = s.brick[par] != 0;
   int lmax = 0;
   if (r < KPS) {
     const PrimTC pr = a.prim[stage_k + r];
     const int at = pr.meta >> 12;
     const StagePrim q = stage_prim(pr, s.off[par * a.w.natom + at], s.offl[par * a.w.natom + at], rad);
     rows[r].o = make_float4(q.ox, q.oy, q.oz, q.g);
-    rows[r].l = make_float4(q.lx, q.ly, q.lz, q.t);
+    // point-list tiles: the cutoff as dran^2 (chi10_exact); brick tiles: q.t
+    rows[r].l = make_float4(q.lx, q.ly, q.lz, brick ? q.t : (pr.dran > 0.f ? pr.dran * pr.dran : -1.f));
     rows[r].c = make_float4(q.al2e, q.alpha, __int_as_float(q.lp), __int_as_float(q.direct));
+    if (!brick) {
+      const double4 A = a.w.atoms[at];
+      rowsd[r] = make_double4(A.x, A.y, A.z, (double)pr.alpha + (double)pr.alpha_lo);
+    }
     lmax = max(q.lp & 15, max((q.lp >> 4) & 15, (q.lp >> 8) & 15));
   }
   lmax = __reduce_max_sync(0xffffffffu, lmax);  // also orders the row writes before the reads
   // the buffer wait is taken inside the first half, before its stores
   bool ok = true;
-  if (s.brick[par]) {
+  if (brick) {
     const float4 *dlt = s.dl + par * 32;
     for (int half = 0; half < 2 && ok; half++, bw.need = false) {
       if (lmax <= 3) ok = produce_half_brick<KIND, false>(rows, half, d, dst, tab, dlt, bw);
@@ -638,8 +705,8 @@ __device__ __forceinline__ bool produce(const TcArgs &a, const Smem &s, int par,
     }
   } else {
     for (int half = 0; half < 2 && ok; half++, bw.need = false) {
-      if (lmax <= 3) ok = produce_half<KIND, false>(rows, half, d, dst, bw);
-      else ok = produce_half<KIND, true>(rows, half, d, dst, bw);
+      if (lmax <= 3) ok = produce_half<KIND, false>(rows, rowsd, half, d, dst, bw);
+      else ok = produce_half<KIND, true>(rows, rowsd, half, d, dst, bw);
     }
   }
   __syncwarp();
@@ -809,11 +876,18 @@ __device__ __forceinline__ void put_point(const TcArgs &a, const Sink &sink, lon
   }
 }
 
+// s + e = a + b exactly (Knuth's two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
 // ------------------------------------------------------------------ kernel
 template <int KIND, class Src, class Sink>
 __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink, int ntiles) {
   extern __shared__ uint8_t smem_raw[];
-  const Smem s = carve(smem_raw, a.w.natom, a.maskw);
+  const Smem s = carve(smem_raw, a);
   constexpr int KPS = KIND == 0 ? 16 : 8;
   constexpr int ESZ = KIND == 0 ? 2 : 4;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -859,11 +933,12 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       for (int mt = 0; mt < a.nmt; mt++) {
         const uint32_t uu = (uint32_t)tt * (uint32_t)a.nmt + (uint32_t)mt;
         if (!warp_wait(s, K::B_EPIFULL, uu & 1, a.err)) return false;
-        float v4[10];
+        // the four quadrants' partial sums of the point, summed in FP64
+        double v4[10];
 #pragma unroll
         for (int k = 0; k < 10; k++) {
           const int i = (p >> 3) * 80 + k * 8 + (p & 7);
-          v4[k] = ((s.part[i] + s.part[320 + i]) + s.part[640 + i]) + s.part[960 + i];
+          v4[k] = ((double)s.part[i] + (double)s.part[320 + i]) + ((double)s.part[640 + i] + (double)s.part[960 + i]);
         }
         const long idx = s.idx[pp * 32 + p];
         const double *xp = s.x + (pp * 32 + p) * 3;
@@ -871,7 +946,7 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           if (idx >= 0) put_point(a, sink, idx, v4, 1, xp);
         } else {
 #pragma unroll
-          for (int k = 0; k < 10; k++) s.acc[k * 32 + p] += (double)v4[k];
+          for (int k = 0; k < 10; k++) s.acc[k * 32 + p] += v4[k];
           if (mt == a.nmt - 1) {
             if (idx >= 0) put_point(a, sink, idx, s.acc + p, 32, xp);
 #pragma unroll
@@ -1060,7 +1135,8 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       }
       // drain outstanding MMAs before the teardown
       ptx::mma_commit(&s.bar[K::B_DRAIN]);
-      ptx::mbar_wait(&s.bar[K::B_DRAIN], 0, K::TIMEOUT_NS);
+      // (a bound of its own: tensor memory is freed only after the MMAs end)
+      ptx::mbar_wait(&s.bar[K::B_DRAIN], 0, s.wait_ns > 2000000000ull ? s.wait_ns : 2000000000ull);
     }
   } else if (warp >= K::W_PROD0) {
     // -------------------------------------------------------- basis block
@@ -1076,6 +1152,10 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       d.x2 = 2.f * d4.x, d.y2 = 2.f * d4.y, d.z2 = 2.f * d4.z;
       d.dd = fmaf(d4.x, d4.x, fmaf(d4.y, d4.y, d4.z * d4.z));
       d.valid = d4.w > 0.f;
+      {
+        const double *xp = s.x + (par * 32 + lane) * 3;
+        d.px = xp[0], d.py = xp[1], d.pz = xp[2];
+      }
       const float rad = s.rad[par];
       const uint16_t *list = s.list + par * a.maskw * 32;
       const int nact = s.nact[par];
@@ -1085,10 +1165,10 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           const int sk = list[j];
           const int b = g % K::NSTAGE;
           const int eb = K::B_EMPTY + b;
-          const BufWait bw{&s.bar[eb], s.abort, a.err, ((g / K::NSTAGE) - 1) & 1u, 1 << (eb < 31 ? eb : 31),
+          const BufWait bw{&s.bar[eb], s.abort, a.err, s.wait_ns, ((g / K::NSTAGE) - 1) & 1u, 1 << (eb < 31 ? eb : 31),
                            g >= (uint32_t)K::NSTAGE};
           if (!(ok = produce<KIND>(a, s, par, sk * KPS, s.stage + b * K::STAGE, d, rad, s.rows + pw * 16,
-                                   s.tab + pw * K::TAB, bw)))
+                                   s.rowsd + pw * 16, s.tab + pw * K::TAB, bw)))
             break;
           ptx::fence_proxy_async_smem();
           __syncwarp();
@@ -1164,8 +1244,17 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
             ptx::tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-              const float p0 = ((__uint_as_float(v[0][j]) + __uint_as_float(dv[0][j])) +
-                                (__uint_as_float(dv[1][j]) + __uint_as_float(dv[2][j]))) + __uint_as_float(xv[j]);
+              // phi: the value accumulators summed exactly (two-sums), the
+              // cross products (2^-11 of phi and below) added to the low part,
+              // rounded once
+              float sh = __uint_as_float(v[0][j]), sl = __uint_as_float(xv[j]);
+#pragma unroll
+              for (int c = 0; c < K::NVACC - 1; c++) {
+                float e;
+                two_sum(sh, __uint_as_float(dv[c][j]), sh, e);
+                sl += e;
+              }
+              const float p0 = sh + sl;
               const float px = __uint_as_float(v[1][j]);
               const float py = __uint_as_float(v[2][j]);
               const float pz = __uint_as_float(v[3][j]);
@@ -1215,11 +1304,6 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
   }
 }
 
-__global__ void k_zero_cgrad(double *cgrad, const int *idx, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) cgrad[idx[i]] = 0.0;
-}
-
 // Scratch of the no-allocation NCI entry: the FP64 re-check list (one slot
 // per grid point, kNoAllocMaxPoints points at most) followed by its
 // counter.  Lives in the module's static device memory, so the entry needs
@@ -1230,25 +1314,38 @@ static __device__ __align__(256) int g_noalloc_scratch[kNoAllocMaxPoints + kNoAl
 
 // Nucleus rule on a split-precision grid, located on the device: grid
 // points within 1e-5 bohr of a nucleus get s = 0 (src/fieldmod@proc.f90:
-// 1148-1154).  inv is the inverse of xmat (column-major).
+// 1148-1154; the same test, d^2 <= 1e-10, as the FP64 NCI sink).  One
+// thread per atom; inv is the inverse of xmat (column-major), so a ball of
+// radius 1e-5 around the nucleus spans fractional index c within
+// 1e-5 * |row c of inv|.  Every grid point in that index box is tested (at
+// most 8 per axis: exact for grid steps above 2.5e-6 bohr).  Grid points are
+// taken as given, not wrapped into the molecular cell: the same for grids
+// inside the cell, which is where critic2's NCI grids lie for molecules.
 __global__ void k_nucleus_cgrad(const double4 *atoms, int natom, GridSpec g, Mat3 inv, double *cgrad) {
   const int at = blockIdx.x * blockDim.x + threadIdx.x;
   if (at >= natom) return;
   const double4 A = atoms[at];
   const double r[3] = {A.x - g.x0[0], A.y - g.x0[1], A.z - g.x0[2]};
-  long ii[3];
+  long lo[3], hi[3];
   for (int c = 0; c < 3; c++) {
     const double f = inv.m[c] * r[0] + inv.m[3 + c] * r[1] + inv.m[6 + c] * r[2];
-    ii[c] = llrint(f);
-    if (ii[c] < 0 || ii[c] >= g.nstep[c]) return;
+    const double rc = 1e-5 * sqrt(inv.m[c] * inv.m[c] + inv.m[3 + c] * inv.m[3 + c] + inv.m[6 + c] * inv.m[6 + c]);
+    const double fl = ceil(f - rc), fh = floor(f + rc);
+    if (!(fh >= 0.0) || !(fl <= (double)(g.nstep[c] - 1)) || fh < fl) return;
+    lo[c] = (long)fmax(fl, 0.0);
+    hi[c] = min((long)fmin(fh, (double)(g.nstep[c] - 1)), lo[c] + 7);
   }
-  double d2 = 0.0;
   const double xyz[3] = {A.x, A.y, A.z};
-  for (int c = 0; c < 3; c++) {
-    const double x = g.x0[c] + ii[0] * g.xmat[c] + ii[1] * g.xmat[3 + c] + ii[2] * g.xmat[6 + c];
-    d2 += (x - xyz[c]) * (x - xyz[c]);
-  }
-  if (sqrt(d2) <= 1e-5) cgrad[(ii[0] * g.nstep[1] + ii[1]) * g.nstep[2] + ii[2]] = 0.0;
+  for (long i = lo[0]; i <= hi[0]; i++)
+    for (long j = lo[1]; j <= hi[1]; j++)
+      for (long k = lo[2]; k <= hi[2]; k++) {
+        double d2 = 0.0;
+        for (int c = 0; c < 3; c++) {
+          const double x = g.x0[c] + i * g.xmat[c] + j * g.xmat[3 + c] + k * g.xmat[6 + c];
+          d2 += (x - xyz[c]) * (x - xyz[c]);
+        }
+        if (d2 <= 1e-10) cgrad[(i * g.nstep[1] + j) * g.nstep[2] + k] = 0.0;
+      }
 }
 
 // ------------------------------------------------------------------- host
@@ -1413,6 +1510,7 @@ TcArgs make_args(Handle &h, int kind) {
   // sign(lambda2) can only be wrong well below these thresholds.
   a.recheck_rel = (float)(t->recheck_rel >= 0.0 ? t->recheck_rel : (kind == 1 ? 1e-4 : 1e-3));
   a.stage_count = nullptr;
+  a.wait_ns = t->wait_ns;
   return a;
 }
 
@@ -1423,23 +1521,60 @@ int sm_count() {
   return n;
 }
 
-template <int KIND, class Src, class Sink>
-void launch_tc(const TcArgs &a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st) {
-  if (ntiles <= 0) return;
+constexpr size_t kSmemLimit = 227 * 1024;
+
+// Shared memory of a launch; whether the per-tile atom tables fit in it.
+size_t tc_smem(const TcArgs &a, bool &atoms_smem) {
   size_t offs[15];
-  const size_t bytes = smem_bytes(a.w.natom, a.maskw, offs);
-  if (bytes > 227 * 1024) fail(C2G_ERR_UNSUPPORTED, "molecule too large for the split-precision kernel's shared memory");
+  size_t bytes = smem_bytes(a.w.natom, a.maskw, true, offs);
+  atoms_smem = bytes <= kSmemLimit;
+  if (!atoms_smem) bytes = smem_bytes(a.w.natom, a.maskw, false, offs);
+  if (bytes > kSmemLimit)
+    fail(C2G_ERR_UNSUPPORTED, "too many primitives for the split-precision kernel's shared memory");
+  return bytes;
+}
+
+template <int KIND, class Src, class Sink>
+void launch_tc(const TcArgs &a, const Src &src, const Sink &sink, int ntiles, int grid, size_t bytes,
+               cudaStream_t st) {
   auto fn = k_tc<KIND, Src, Sink>;
   C2G_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  const int grid = std::min(ntiles, sm_count());
   fn<<<grid, K::NTHR, bytes, st>>>(a, src, sink, ntiles);
   C2G_CUDA(cudaGetLastError());
 }
 
+// Launches the split kernel over ntiles 32-point tiles, one CTA per SM at
+// most.  Molecules whose per-tile atom tables do not fit shared memory get
+// them in a per-CTA slice of a global buffer owned by the handle (grown on
+// demand); with allow_alloc false (the no-allocation entry) such molecules
+// are refused.
 template <class Src, class Sink>
-void launch_kind(int kind, const TcArgs &a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st) {
-  if (kind == 0) launch_tc<0>(a, src, sink, ntiles, st);
-  else launch_tc<1>(a, src, sink, ntiles, st);
+void launch_kind(Handle &h, int kind, TcArgs a, const Src &src, const Sink &sink, int ntiles, cudaStream_t st,
+                 bool allow_alloc = true) {
+  if (ntiles <= 0) return;
+  const int grid = std::min(ntiles, sm_count());
+  bool atoms_smem = true;
+  a.atab = nullptr;
+  a.atab_stride = atom_table_bytes(a.w.natom);
+  tc_smem(a, atoms_smem);
+  if (!atoms_smem) {
+    if (!allow_alloc)
+      fail(C2G_ERR_UNSUPPORTED, "molecule too large for the no-allocation entry (" + std::to_string(a.w.natom) +
+                                    " atoms: the per-tile atom tables do not fit shared memory)");
+    TcOperands *t = h.tc;
+    const size_t need = a.atab_stride * (size_t)grid;
+    if (t->atab_cap < need) {
+      if (t->atab) cudaFree(t->atab);
+      t->atab = nullptr;
+      t->atab_cap = 0;
+      if (cudaMalloc(&t->atab, need) != cudaSuccess) fail(C2G_ERR_ALLOC, "cudaMalloc (atom tables)");
+      t->atab_cap = need;
+    }
+    a.atab = t->atab;
+  }
+  const size_t bytes = tc_smem(a, atoms_smem);
+  if (kind == 0) launch_tc<0>(a, src, sink, ntiles, grid, bytes, st);
+  else launch_tc<1>(a, src, sink, ntiles, grid, bytes, st);
 }
 
 void check_device_error(TcOperands *t) {
@@ -1449,6 +1584,27 @@ void check_device_error(TcOperands *t) {
     C2G_CUDA(cudaMemset(t->err, 0, sizeof(int)));
     fail(C2G_ERR_CUDA, "split-precision kernel: a pipeline wait timed out (mask " + std::to_string(e) + ")");
   }
+}
+
+// Launches the nucleus rule for a grid on the stream (nothing when xmat is
+// singular or the molecule has no atoms).
+void launch_nucleus_rule(const Handle &h, const GridSpec &g, double *d_cgrad, cudaStream_t st) {
+  const double *M = g.xmat;
+  const double det = M[0] * (M[4] * M[8] - M[7] * M[5]) - M[3] * (M[1] * M[8] - M[7] * M[2]) +
+                     M[6] * (M[1] * M[5] - M[4] * M[2]);
+  if (det == 0.0 || h.dev.natom <= 0) return;
+  Mat3 inv;
+  inv.m[0] = (M[4] * M[8] - M[5] * M[7]) / det;
+  inv.m[3] = (M[5] * M[6] - M[3] * M[8]) / det;
+  inv.m[6] = (M[3] * M[7] - M[4] * M[6]) / det;
+  inv.m[1] = (M[2] * M[7] - M[1] * M[8]) / det;
+  inv.m[4] = (M[0] * M[8] - M[2] * M[6]) / det;
+  inv.m[7] = (M[1] * M[6] - M[0] * M[7]) / det;
+  inv.m[2] = (M[1] * M[5] - M[2] * M[4]) / det;
+  inv.m[5] = (M[2] * M[3] - M[0] * M[5]) / det;
+  inv.m[8] = (M[0] * M[4] - M[1] * M[3]) / det;
+  k_nucleus_cgrad<<<(h.dev.natom + 127) / 128, 128, 0, st>>>(h.dev.atoms, h.dev.natom, g, inv, d_cgrad);
+  C2G_CUDA(cudaGetLastError());
 }
 
 }  // namespace
@@ -1494,10 +1650,13 @@ void tc_destroy(TcOperands *t) {
   if (!t) return;
   for (void *p : t->allocs) cudaFree(p);
   if (t->scratch) cudaFree(t->scratch);
+  if (t->atab) cudaFree(t->atab);
   delete t;
 }
 
 void tc_set_recheck(Handle &h, double rel) { h.tc->recheck_rel = rel; }
+
+void tc_set_wait_ns(Handle &h, uint64_t ns) { h.tc->wait_ns = ns; }
 
 void tc_check_error(Handle &h) { check_device_error(h.tc); }
 
@@ -1505,7 +1664,7 @@ void tc_points(Handle &h, int prec, int n, const double *d_xyz, double *d_rec, c
   const int kind = kind_of(prec);
   TcArgs a = make_args(h, kind);
   ListSrc src{d_xyz, n, wrap};
-  launch_kind(kind, a, src, TcRecSink{d_rec}, (n + 31) / 32, st);
+  launch_kind(h, kind, a, src, TcRecSink{d_rec}, (n + 31) / 32, st);
   C2G_CUDA(cudaStreamSynchronize(st));
   check_device_error(h.tc);
 }
@@ -1515,7 +1674,7 @@ void tc_points_index(Handle &h, int prec, const double *d_x, const int *d_idx, c
   const int kind = kind_of(prec);
   TcArgs a = make_args(h, kind);
   IndexSrc src{d_x, d_idx, d_count};
-  launch_kind(kind, a, src, TcRecSink{d_rec}, (maxn + 31) / 32, st);
+  launch_kind(h, kind, a, src, TcRecSink{d_rec}, (maxn + 31) / 32, st);
 }
 
 long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double *d_cgrad, cudaStream_t st,
@@ -1544,58 +1703,12 @@ long tc_nci_grid(Handle &h, int prec, const GridSpec &g, double *d_crho, double 
   a.recheck_cap = (int)npts;
   GridSrc src{g, (g.nstep[1] + 3) / 4, (g.nstep[2] + 7) / 8};
   const long ntiles = (long)g.nstep[0] * src.ntj * src.ntk;
-  launch_kind(kind, a, src, TcNciSink{d_crho, d_cgrad}, (int)ntiles, st);
+  launch_kind(h, kind, a, src, TcNciSink{d_crho, d_cgrad}, (int)ntiles, st);
   if (ev_split) C2G_CUDA(cudaEventRecord(ev_split, st));
   // FP64 re-evaluation of the listed points (the count is read on device)
   launch_fp64_nci_list(h.dev, g, scratch, count, (int)npts, d_crho, d_cgrad, st);
   // nucleus rule: |grad| := 0 (s = 0) at grid points within 1e-5 bohr of a nucleus
-  std::vector<int> nuc;
-  {
-    const HostWfn &w = h.host;
-    // invert xmat (columns = axis steps) to locate each nucleus on the grid
-    const double *M = g.xmat;
-    const double det = M[0] * (M[4] * M[8] - M[7] * M[5]) - M[3] * (M[1] * M[8] - M[7] * M[2]) +
-                       M[6] * (M[1] * M[5] - M[4] * M[2]);
-    if (det != 0.0) {
-      double inv[9];
-      inv[0] = (M[4] * M[8] - M[5] * M[7]) / det;
-      inv[3] = (M[5] * M[6] - M[3] * M[8]) / det;
-      inv[6] = (M[3] * M[7] - M[4] * M[6]) / det;
-      inv[1] = (M[2] * M[7] - M[1] * M[8]) / det;
-      inv[4] = (M[0] * M[8] - M[2] * M[6]) / det;
-      inv[7] = (M[1] * M[6] - M[0] * M[7]) / det;
-      inv[2] = (M[1] * M[5] - M[2] * M[4]) / det;
-      inv[5] = (M[2] * M[3] - M[0] * M[5]) / det;
-      inv[8] = (M[0] * M[4] - M[1] * M[3]) / det;
-      for (int at = 0; at < w.natom; at++) {
-        double r[3], f[3];
-        for (int c = 0; c < 3; c++) r[c] = w.xyz[3 * at + c] - g.x0[c];
-        for (int c = 0; c < 3; c++) f[c] = inv[c] * r[0] + inv[3 + c] * r[1] + inv[6 + c] * r[2];
-        long ii[3];
-        bool inside = true;
-        for (int c = 0; c < 3; c++) {
-          ii[c] = std::lround(f[c]);
-          if (ii[c] < 0 || ii[c] >= g.nstep[c]) inside = false;
-        }
-        if (!inside) continue;
-        double d2 = 0.0;
-        for (int c = 0; c < 3; c++) {
-          const double x = g.x0[c] + ii[0] * M[c] + ii[1] * M[3 + c] + ii[2] * M[6 + c];
-          d2 += (x - w.xyz[3 * at + c]) * (x - w.xyz[3 * at + c]);
-        }
-        if (std::sqrt(d2) <= 1e-5) nuc.push_back((int)((ii[0] * g.nstep[1] + ii[1]) * g.nstep[2] + ii[2]));
-      }
-    }
-  }
-  if (!nuc.empty()) {
-    int *dn = nullptr;
-    C2G_CUDA(cudaMalloc(&dn, sizeof(int) * nuc.size()));
-    C2G_CUDA(cudaMemcpyAsync(dn, nuc.data(), sizeof(int) * nuc.size(), cudaMemcpyHostToDevice, st));
-    k_zero_cgrad<<<((int)nuc.size() + 127) / 128, 128, 0, st>>>(d_cgrad, dn, (int)nuc.size());
-    C2G_CUDA(cudaGetLastError());
-    C2G_CUDA(cudaStreamSynchronize(st));
-    cudaFree(dn);
-  }
+  launch_nucleus_rule(h, g, d_cgrad, st);
   int hcount = 0;
   unsigned long long hstages = 0;
   C2G_CUDA(cudaMemcpyAsync(&hcount, count, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1646,25 +1759,9 @@ void tc_nci_grid_noalloc(Handle &h, int prec, const GridSpec &g, double *d_crho,
   a.recheck_cap = (int)npts;
   GridSrc src{g, (g.nstep[1] + 3) / 4, (g.nstep[2] + 7) / 8};
   const long ntiles = (long)g.nstep[0] * src.ntj * src.ntk;
-  launch_kind(kind, a, src, TcNciSink{d_crho, d_cgrad}, (int)ntiles, st);
+  launch_kind(h, kind, a, src, TcNciSink{d_crho, d_cgrad}, (int)ntiles, st, false);
   launch_fp64_nci_list(h.dev, g, scratch, count, (int)npts, d_crho, d_cgrad, st);
-  const double *M = g.xmat;
-  const double det = M[0] * (M[4] * M[8] - M[7] * M[5]) - M[3] * (M[1] * M[8] - M[7] * M[2]) +
-                     M[6] * (M[1] * M[5] - M[4] * M[2]);
-  if (det != 0.0 && h.dev.natom > 0) {
-    Mat3 inv;
-    inv.m[0] = (M[4] * M[8] - M[5] * M[7]) / det;
-    inv.m[3] = (M[5] * M[6] - M[3] * M[8]) / det;
-    inv.m[6] = (M[3] * M[7] - M[4] * M[6]) / det;
-    inv.m[1] = (M[2] * M[7] - M[1] * M[8]) / det;
-    inv.m[4] = (M[0] * M[8] - M[2] * M[6]) / det;
-    inv.m[7] = (M[1] * M[6] - M[0] * M[7]) / det;
-    inv.m[2] = (M[1] * M[5] - M[2] * M[4]) / det;
-    inv.m[5] = (M[2] * M[3] - M[0] * M[5]) / det;
-    inv.m[8] = (M[0] * M[4] - M[1] * M[3]) / det;
-    k_nucleus_cgrad<<<(h.dev.natom + 127) / 128, 128, 0, st>>>(h.dev.atoms, h.dev.natom, g, inv, d_cgrad);
-    C2G_CUDA(cudaGetLastError());
-  }
+  launch_nucleus_rule(h, g, d_cgrad, st);
   // pipeline timeouts of the split kernel are reported by this call
   int e = 0;
   C2G_CUDA(cudaMemcpyAsync(&e, t->err, sizeof(int), cudaMemcpyDeviceToHost, st));

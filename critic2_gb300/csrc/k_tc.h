@@ -13,6 +13,10 @@ void tc_destroy(TcOperands *t);
 // re-evaluated in FP64.
 void tc_set_recheck(Handle &h, double rel);
 
+// Limit (nanoseconds) of every pipeline wait of the split kernel; a wait
+// that runs out ends the launch with C2G_ERR_CUDA.
+void tc_set_wait_ns(Handle &h, uint64_t ns);
+
 // Reports (and clears) a pipeline timeout recorded by an earlier split kernel.
 void tc_check_error(Handle &h);
 

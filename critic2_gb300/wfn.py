@@ -115,6 +115,12 @@ class Wavefunction:
         |grad| (C2G_PARAM_NEWTON_STALL; 0 = off, critic2's semantics)."""
         L.check(L.lib().c2g_wfn_set_param(self._h, 2, float(k)))
 
+    def set_wait_ns(self, ns: float):
+        """Limit (ns) of every pipeline wait of the split-precision kernel
+        (C2G_PARAM_WAIT_NS, default 4e9); a wait that runs out makes the call
+        fail with C2G_ERR_CUDA and leaves the handle usable."""
+        L.check(L.lib().c2g_wfn_set_param(self._h, 3, float(ns)))
+
     # ------------------------------------------------------------ rho2/grd
     def rho2(self, xyz, nder: int = 2, prec="fp64") -> dict:
         """molwfn%rho2 at points xyz (n,3).  Arrays are per point:

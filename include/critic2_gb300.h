@@ -153,6 +153,15 @@ int c2g_wfn_set_edf(c2g_wfn *h, int nedf, const int *icenter, const int *itype, 
                                     gfnormeps and would otherwise run to maxit;
                                     this option has no counterpart in the
                                     reference. */
+#define C2G_PARAM_WAIT_NS 3 /* split-precision kernel: limit, in nanoseconds,
+                               of every wait between its pipeline stages
+                               (default 4e9).  A wait that runs out stops the
+                               kernel cleanly (its MMAs in flight are
+                               drained, its tensor memory is freed) and the
+                               call returns C2G_ERR_CUDA with "a pipeline
+                               wait timed out"; the handle stays usable.
+                               Range [1, 6e11]; this option has no
+                               counterpart in the reference. */
 int c2g_wfn_set_param(c2g_wfn *h, int param, double value);
 
 /* Sizes after pruning. */
@@ -221,9 +230,9 @@ int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int 
  * sizes everything at start-up) and codes that stream grid slabs on their
  * own streams, where cudaFree -- which synchronises the whole device --
  * would stall their other work.  c2g_nciplot_dev allocates its FP64
- * re-check list and a nucleus list; this entry keeps the re-check list in a
- * static device array of 4 MiB + 256 B and applies the nucleus rule on the
- * device, and makes no cudaMalloc/cudaFree or allocating-library call.
+ * re-check list (kept on the handle, grown on demand); this entry keeps the
+ * re-check list in a static device array of 4 MiB + 256 B, and makes no
+ * cudaMalloc/cudaFree or allocating-library call.
  *   - At most C2G_NOALLOC_MAX_POINTS grid points per call; larger grids are
  *     rejected with C2G_ERR_ARG (split them into i-slabs and call per slab).
  *   - The split operands of the requested mode must already be on the
@@ -232,7 +241,14 @@ int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int 
  *     the call returns C2G_ERR_UNSUPPORTED.  C2G_PREC_FP64 needs nothing.
  *   - The first call on each device looks up the scratch array's address
  *     (cudaGetSymbolAddress, with that device current); make that first
- *     call before any stream capture.
+ *     call before any stream capture.  That first call (like the first call
+ *     of any entry, with CUDA's default lazy module loading) also loads the
+ *     library's GPU code together with the 4 MiB static array, which takes
+ *     device memory once: make it before a pool of the caller's reserves
+ *     the GPU's memory.
+ *   - The address is kept per device ordinal for the life of the process.
+ *     After cudaDeviceReset (or any teardown of the device's primary
+ *     context) it is stale: do not call this entry again in that process.
  *   - The re-check counter, which must start at zero, is cleared by the call
  *     itself on the given stream.
  *   - The scratch is shared by all calls on a device: calls that overlap in

@@ -9,13 +9,15 @@ line must be reproduced exactly from its parsed numbers), the body layout
 and the cutoff pass (s = 100 wherever |sign(lambda2) rho * 100| > 10),
 without the reference tree.
 
-    python tests/golden/make_cube_golden.py [reference-root]
+    python tests/golden/make_cube_golden.py <reference-root>
 """
 import json
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_cube_golden.py <reference-root>")
+REF = sys.argv[1]
 D = os.path.join(REF, "tests", "015_grdplot", "ref")
 HERE = os.path.dirname(os.path.abspath(__file__))
 

@@ -10,8 +10,8 @@ distributed with the source, so the records pin the field's
 post-processing (eigen-solve, rank/signature, |grad|, Laplacian, spin
 halves), not the evaluator itself.
 
-Run from the repository root with the critic2 source tree at
-/root/reference:  python tests/golden/make_golden.py
+Run from the repository root, giving the root of a critic2 source tree:
+    python tests/golden/make_golden.py <reference-root>
 Writes tests/golden/point_records.json.
 """
 from __future__ import annotations
@@ -20,8 +20,11 @@ import glob
 import json
 import os
 import re
+import sys
 
-REF = "/root/reference/tests"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <reference-root>")
+REF = os.path.join(sys.argv[1], "tests")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "point_records.json")
 
 NUM = r"[-+]?\d*\.\d+(?:[EeDd][-+]?\d+)?"

@@ -1,13 +1,16 @@
 """Writes point_line_benzene.json: critic2's own POINT block and LINE file
 for benzene (tests/004_load/ref/002_load-wfx.cro lines of `point 0.1 0.2
 0.3`, and 002_load-wfx.line of `line 0 -4 0 0 4 0 101`), the format pins of
-critic2_gb300.rhoplot.  Run here, where the reference tree is present:
-    python tests/golden/make_point_line.py
+critic2_gb300.rhoplot.  Give the root of a critic2 source tree:
+    python tests/golden/make_point_line.py <reference-root>
 """
 import json
 import os
+import sys
 
-REF = "/root/reference/tests/004_load/ref"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_point_line.py <reference-root>")
+REF = os.path.join(sys.argv[1], "tests", "004_load", "ref")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -3,13 +3,16 @@ read_fchk and read_molden (dsphcar, fsphcar, gsphcar_fchk, gsphcar;
 src/wfn_private@proc.F90:46-167),
 parsed from the reference source with its named sqrt constants resolved,
 as T[m][c] (m = 0, 1, -1, ...; Cartesian components in fchk order).
-Run in the build container (it reads the reference tree):
-    python make_sphcar.py /root/reference/src/wfn_private@proc.F90"""
+Give the reference's source file (src/wfn_private@proc.F90 of a critic2
+source tree):
+    python make_sphcar.py <reference-root>/src/wfn_private@proc.F90"""
 import json
 import math
 import re
 import sys
 
+if len(sys.argv) != 2:
+    sys.exit("usage: make_sphcar.py <path of wfn_private@proc.F90>")
 src = open(sys.argv[1]).read()
 const = {}
 for name, expr in re.findall(r"real\*8, parameter :: (\w+) = ([^\n!]+)", src):

@@ -2,7 +2,7 @@
 records incl. spin channels, grd, NCI grid, Newton), the split-precision
 NCI grid against the FP64 one, the wfx EDF sections and c2g_wfn_set_edf.
 Bars: FP64 1e-10 relative; the split modes keep the bars of the core-free
-split tests (TF32x3 |drho|/rho 5e-6, |ds| 1e-3; BF16x3 5e-5, 1e-2)."""
+split tests (TF32x3 |drho|/rho 1e-6, |ds| 1e-3; BF16x3 5e-5, 1e-2)."""
 import dataclasses
 
 import numpy as np
@@ -105,7 +105,7 @@ def test_nci_fp64_with_core(gpu_lib, oracle_mod, mol_edf, grid_edf):
 
 
 # split-precision bars of the core-free tests (|drho|/rho, |ds|)
-TOL = {"tf32x3": dict(rho=5e-6, s=1e-3), "bf16x3": dict(rho=5e-5, s=1e-2)}
+TOL = {"tf32x3": dict(rho=1e-6, s=1e-3), "bf16x3": dict(rho=5e-5, s=1e-2)}
 
 
 @pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])

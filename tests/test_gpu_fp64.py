@@ -219,6 +219,53 @@ def test_autocritic(pair12):
         assert list(res["counts"]) == list(ref["counts"]) and res["ph"] == ref["ph"]
 
 
+def test_autocritic_cp100_vs_oracle(gpu_lib, oracle_mod):
+    """cp100 (100 atoms, 22,160 pair seeds), FP64 AUTO on the GPU against
+    the oracle's.  critic2 declares Newton converged at an absolute
+    |grad rho| < 1e-12 (src/fieldmod@proc.f90:2256), which on these
+    densities (rho up to 1e3) lies on the FP64 rounding floor of |grad rho|:
+    the two evaluators' summation orders put a CP on either side of it.
+    So the CP lists are compared up to that floor: every CP one search lists
+    and the other does not is a CP of the other's own field (|grad rho| <=
+    1e-10 there, same rank 3 and signature), and the other's Newton with
+    gfnormeps 1e-10 converges from it without moving more than 1e-8 bohr.
+    CPs found by both have the same type and density (1e-10)."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("cp100")
+    g, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    res = g.autocritic(prec="fp64")
+    ref = o.autocritic()
+    nat = mol.natom
+    gx, ox = res["xyz"][nat:], ref["xyz"][nat:]
+    gt, ot = res["typ"][nat:], ref["typ"][nat:]
+    d = np.linalg.norm(gx[:, None, :] - ox[None, :, :], axis=2)
+    gi = d.argmin(1) if len(ox) else np.zeros(len(gx), int)
+    in_ref = d.min(1) < 1e-2 if len(ox) else np.zeros(len(gx), bool)
+    in_res = d.min(0) < 1e-2 if len(gx) else np.zeros(len(ox), bool)
+    for i in np.nonzero(in_ref)[0]:
+        j = gi[i]
+        assert gt[i] == ot[j]
+        assert abs(res["f"][nat + i] - ref["f"][nat + j]) <= 1e-10 * abs(ref["f"][nat + j])
+    # found by the GPU only: CPs of the oracle's field to its rounding floor
+    only_g = gx[~in_ref]
+    for x, t in zip(only_g, gt[~in_ref]):
+        r = o.grd(x, 2)
+        assert r.gfmod <= 1e-10 and r.r == 3 and r.s == t
+    xo, ier = o.newton_batch(only_g, 1e-10)
+    assert np.all(ier == 0) and np.linalg.norm(xo - only_g, axis=1).max() <= 1e-8
+    # found by the oracle only: CPs of the GPU's field to its rounding floor
+    only_o = ox[~in_res]
+    if len(only_o):
+        q = g.grd(only_o, 2, "fp64")
+        assert np.all(q["gfmod"] <= 1e-10) and np.all(q["r"] == 3) and np.all(q["s"] == ot[~in_res])
+        xg, ierg = g.newton(only_o, 1e-10)
+        assert np.all(ierg == 0) and np.linalg.norm(xg - only_o, axis=1).max() <= 1e-8
+    # nearly every oracle CP is found by the GPU
+    assert in_res.mean() >= 0.95
+    print(f"\ncp100: GPU {len(gx)} non-nuclear CPs (PH {res['ph']}), oracle {len(ox)} (PH {ref['ph']}), "
+          f"{int(in_ref.sum())} common, GPU-only {len(only_g)}, oracle-only {len(only_o)}")
+
+
 def test_error_paths(pair12, gpu_lib):
     g, _ = pair12
     with pytest.raises(gpu_lib.C2GError) as e:

@@ -12,9 +12,9 @@ from critic2_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
-# measured levels with a margin; the bench reports the NCI-grid errors
-# against the spec bars (|drho|/rho <= 1e-6, |ds| <= 1e-3)
-TOL = {"tf32x3": dict(rho=5e-6, grad=2e-5, s=1e-3), "bf16x3": dict(rho=5e-5, grad=1e-3, s=1e-2)}
+# TF32x3: the spec bars (|drho|/rho <= 1e-6, |ds| <= 1e-3); BF16x3, a
+# documented alternative that does not meet them, at its measured level
+TOL = {"tf32x3": dict(rho=1e-6, grad=2e-5, s=1e-3), "bf16x3": dict(rho=5e-5, grad=1e-3, s=1e-2)}
 
 
 @pytest.fixture(scope="module")
@@ -178,22 +178,25 @@ def test_g_and_h_shells_split():
     rng = np.random.default_rng(2)
     pts = rng.uniform(m.atom_xyz.min(0), m.atom_xyz.max(0), size=(500, 3))
     r64 = w.rho2(pts, 2, "fp64")
+    # g and h primitives (l up to 5, powers of the offset formed by repeated
+    # FP32 products) on a 0.15-bohr grid: measured 1.3e-6 for TF32x3, held to
+    # 2e-6; the spec configurations are s/p/d/f
+    tol_rho = {"tf32x3": 2e-6, "bf16x3": TOL["bf16x3"]["rho"]}
     for prec in ("tf32x3", "bf16x3"):
         c, s, _ = w.nciplot(x0, xm, ns, prec)
         rho, rho64 = np.abs(c) / 100, np.abs(c64) / 100
-        assert np.max(np.abs(rho - rho64) / rho64) < TOL[prec]["rho"]
+        assert np.max(np.abs(rho - rho64) / rho64) < tol_rho[prec]
         assert np.max(np.abs(s - g64)) < TOL[prec]["s"]
         r = w.rho2(pts, 2, prec)
-        assert np.max(np.abs(r["rho"][:, 0] - r64["rho"][:, 0]) / r64["rho"][:, 0]) < TOL[prec]["rho"]
+        assert np.max(np.abs(r["rho"][:, 0] - r64["rho"][:, 0]) / r64["rho"][:, 0]) < tol_rho[prec]
 
 
 def test_nci60_density_error_distribution(gpu_lib):
     """TF32x3 density against the GPU's FP64 plain form on a 96^3 grid of
-    the 60-atom molecule (885k points): the largest relative error is at
-    the 1e-6 bar (measured 1.003e-6 at one point of the full 200^3 grid,
-    the rest below), the 99.9th percentile about half of it, and the mean
-    signed error (the bias of the truncating accumulation, 4 value
-    accumulators) below 1.5e-7 in size."""
+    the 60-atom molecule (885k points): the largest relative error within
+    the 1e-6 bar, the 99.9th percentile within 5e-7, and the mean signed
+    error (the bias of the tensor core's truncating accumulation, with four
+    value accumulators) below 1.5e-7 in size."""
     from critic2_gb300.wfn import Wavefunction
     mol = synth.make_molecule("nci60")
     w = Wavefunction(mol)
@@ -202,8 +205,8 @@ def test_nci60_density_error_distribution(gpu_lib):
     c32, s32, _ = w.nciplot(x0, xm, ns, "tf32x3")
     r64, r32 = np.abs(c64), np.abs(c32)
     err = np.abs(r32 - r64) / r64
-    assert err.max() <= 1.05e-6
-    assert np.quantile(err, 0.999) <= 6e-7
+    assert err.max() <= 1e-6
+    assert np.quantile(err, 0.999) <= 5e-7
     assert abs(np.mean((r32 - r64) / r64)) <= 1.5e-7
     assert np.abs(s32 - s64).max() <= 1e-3
     assert np.array_equal(np.sign(c32), np.sign(c64))

@@ -41,10 +41,16 @@ def test_noalloc_matches_allocating_entry(setup, prec):
     torch.cuda.synchronize()
     inuc = (20 * ns[1] + 30) * ns[2] + 40
     assert ref_g[inuc].item() == 0.0
-    for _ in range(2):
-        r, g = _bufs(torch, n, dev)
+    outs = [_bufs(torch, n, dev) for _ in range(2)]
+    free = []
+    for r, g in outs:
         w.nciplot_dev_noalloc(x0, xm, ns, prec, r.data_ptr(), g.data_ptr(), stream.cuda_stream)
         torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info(dev)[0])
+    # the second call takes no device memory (the first one may load the
+    # library's GPU code and its static scratch)
+    assert free[1] == free[0]
+    for r, g in outs:
         # same kernels, same arithmetic: equal to the allocating entry
         # (tolerance 1e-12 relative, FP64 outputs)
         assert torch.isfinite(r).all() and torch.isfinite(g).all()
