@@ -62,8 +62,8 @@ TF32_CUBLAS_TFLOPS = 1006.0
 # MMA columns the split kernel issues per active (32-point tile, K-stage)
 # pair and 128-MO tile (M = 128, K = 8 TF32 or 16 BF16): the hi*hi products
 # of the 10 components (320), the cross products of components 1-9 (2 x 288)
-# and the value's three cross products (3 x 32).
-ISSUED_COLUMNS_PER_STAGE = 320 + 2 * 288 + 3 * 32
+# and the value's two cross products (2 x 32).
+ISSUED_COLUMNS_PER_STAGE = 320 + 2 * 288 + 2 * 32
 
 
 def env_int(k, d):
@@ -255,7 +255,8 @@ def cp_search(args):
         st = cpseed.evaluate(mol, net, prec, int(stall))
         out[f"{prec}, newton_stall {stall}"] = {k: st[k] for k in (
             "ms_plain", "ms_learned", "speedup", "recall", "recall_outside_cores", "ncp", "ncp_outside_cores",
-            "plain_ph", "learned_ph", "stage", "reason", "plain_seeds", "learned_seeds", "proposal", "grid_seeds")
+            "plain_ph", "learned_ph", "stage", "reason", "plain_seeds", "learned_seeds", "critic2_seed_list",
+            "proposal", "grid_seeds")
             if k in st}
     # AUTO's graph stage (makegraph: two gradient paths per bond and ring
     # CP) on the FP64 pair-seed CP list, through c2g_cp_graph

@@ -490,17 +490,23 @@ def evaluate(mol, net: SeedNet, prec: str = "fp64", stall: int = 0) -> dict:
     try:
         learned_autocritic(w, net, prec)  # warm-up (first-use allocations)
         ref, ms_plain = timed(w.autocritic, None, prec)
+        # critic2's own seed list (both ordered pairs: every seed twice)
+        ref2, ms_plain2 = timed(w.autocritic, w.pair_seeds(), prec)
         got = learned_autocritic(w, net, prec)
         grid, ms_grid = timed(lambda: w.autocritic(grid_seeds(w), prec))
         prop = got["proposal"]
         out = dict(molecule=mol.name, natom=mol.natom, prec=prec, newton_stall=stall, plain_ph=int(ref["ph"]),
                    plain_seeds=int(ref["nseed"]), ms_plain=round(ms_plain, 1),
+                   critic2_seed_list=dict(seeds=int(ref2["nseed"]), ms=round(ms_plain2, 1),
+                                          same_cps=bool(len(ref2["xyz"]) == len(ref["xyz"]) and
+                                                        np.allclose(ref2["xyz"], ref["xyz"], atol=1e-9))),
                    learned_ph=int(got["ph"]), stage=got["stage"], reason=got["reason"],
                    learned_seeds=int(got["seeds_used"]), ms_learned=round(got["ms"], 1),
                    speedup=round(ms_plain / got["ms"], 2), tries=got["tries"])
         out.update(compare(ref, got, mol.atom_xyz))
         c = compare(ref, prop, mol.atom_xyz)
         out["proposal"] = dict(seeds=prop["seeds"], ms=round(prop["ms"], 1), speedup=round(ms_plain / prop["ms"], 2),
+                               speedup_vs_critic2_seed_list=round(ms_plain2 / prop["ms"], 2),
                                ph=prop["ph"], ncp_found=int(len(prop["xyz"])), recall=c["recall"],
                                recall_outside_cores=c["recall_outside_cores"])
         c = compare(ref, grid, mol.atom_xyz)

@@ -27,10 +27,14 @@ struct Cp {
   int typ, typind;
 };
 
-std::vector<double> pair_seeds(const HostWfn &w, double maxdist, int npts) {
+// critic2's molecular seeds: npts points on every ordered atom pair closer
+// than maxdist.  With distinct, each unordered pair once: the k-th point of
+// i -> j is the (npts + 1 - k)-th point of j -> i, so critic2's list holds
+// every seed twice (equal up to rounding); one of each halves Newton's work.
+std::vector<double> pair_seeds(const HostWfn &w, double maxdist, int npts, bool distinct = false) {
   std::vector<double> out;
   for (int i1 = 0; i1 < w.natom; i1++)
-    for (int i2 = 0; i2 < w.natom; i2++) {
+    for (int i2 = distinct ? i1 + 1 : 0; i2 < w.natom; i2++) {
       if (i1 == i2) continue;
       const double *a = &w.xyz[3 * i1], *b = &w.xyz[3 * i2];
       const double d = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) +
@@ -137,7 +141,7 @@ int c2g_autocritic(c2g_wfn *hp, int nseed, const double *xseed, int prec, int ma
     const HostWfn &w = h->host;
     std::vector<double> seeds;
     if (xseed) seeds.assign(xseed, xseed + 3 * (size_t)std::max(nseed, 0));
-    else seeds = pair_seeds(w, 15.0, 5);
+    else seeds = pair_seeds(w, 15.0, 5, true);  // same CP list as critic2's doubled seed list
     const int ns = (int)(seeds.size() / 3);
     std::vector<int> ier(std::max(ns, 1), 2);
     const double gfnormeps = 1e-12, cpeps = 1e-2, nuceps = 1e-1, nucepsh = 2e-1;

@@ -138,8 +138,9 @@ static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
 constexpr int TAB = 4 * 13;  // axis-factor table: 4 primitives x (1 x + 4 y + 8 z values)
 // barrier slots
+// (the epilogue's partial sums are double-buffered: EPIFULL / EPIFREE per buffer)
 constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17, B_EPIFULL = 18,
-              B_EPIFREE = 19, B_TREADY = 20, B_TFREE = 22, B_DRAIN = 24, NBAR = 25;
+              B_EPIFREE = 20, B_TREADY = 22, B_TFREE = 24, B_DRAIN = 26, NBAR = 27;
 // One producer warp per stage buffer.  The buffer waits are mbarrier parity
 // waits; with more producers than buffers the producer of stage g could wait
 // for stage g - NSTAGE while stage g - 2 NSTAGE still holds the buffer, and
@@ -208,7 +209,7 @@ __host__ __device__ inline size_t smem_bytes(int natom, int maskw, bool atoms_sm
   };
   offs[0] = take((size_t)K::NSTAGE * K::STAGE, 1024);
   offs[1] = take(4 * 32 * K::RED * 4, 16);
-  offs[2] = take(4 * 320 * 4, 16);
+  offs[2] = take(2 * 4 * 320 * 4, 16);
   offs[3] = take(10 * 32 * 8, 16);
   offs[4] = take(2 * 32 * 3 * 8, 16);
   offs[5] = take(2 * 32 * 8, 16);
@@ -900,8 +901,10 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
     for (int b = 0; b < K::NCBUF; b++) ptx::mbar_init(&s.bar[K::B_C + b], 4);
     ptx::mbar_init(&s.bar[K::B_ACCFULL], 1);
     ptx::mbar_init(&s.bar[K::B_ACCEMPTY], 4);
-    ptx::mbar_init(&s.bar[K::B_EPIFULL], 4);
-    ptx::mbar_init(&s.bar[K::B_EPIFREE], 1);
+    for (int p = 0; p < 2; p++) {
+      ptx::mbar_init(&s.bar[K::B_EPIFULL + p], 4);
+      ptx::mbar_init(&s.bar[K::B_EPIFREE + p], 1);
+    }
     for (int p = 0; p < 2; p++) {
       ptx::mbar_init(&s.bar[K::B_TREADY + p], 1);
       ptx::mbar_init(&s.bar[K::B_TFREE + p], K::NPROD + 1 + 4);
@@ -932,13 +935,16 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
       const int p = lane;
       for (int mt = 0; mt < a.nmt; mt++) {
         const uint32_t uu = (uint32_t)tt * (uint32_t)a.nmt + (uint32_t)mt;
-        if (!warp_wait(s, K::B_EPIFULL, uu & 1, a.err)) return false;
+        // partial sums of pass uu in buffer uu & 1
+        const int pb = (int)(uu & 1u);
+        if (!warp_wait(s, K::B_EPIFULL + pb, (uu >> 1) & 1, a.err)) return false;
+        const float *part = s.part + pb * 1280;
         // the four quadrants' partial sums of the point, summed in FP64
         double v4[10];
 #pragma unroll
         for (int k = 0; k < 10; k++) {
           const int i = (p >> 3) * 80 + k * 8 + (p & 7);
-          v4[k] = ((double)s.part[i] + (double)s.part[320 + i]) + ((double)s.part[640 + i] + (double)s.part[960 + i]);
+          v4[k] = ((double)part[i] + (double)part[320 + i]) + ((double)part[640 + i] + (double)part[960 + i]);
         }
         const long idx = s.idx[pp * 32 + p];
         const double *xp = s.x + (pp * 32 + p) * 3;
@@ -954,7 +960,7 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           }
         }
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_EPIFREE]);
+        if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_EPIFREE + pb]);
       }
       return true;
     };
@@ -1219,9 +1225,10 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
         // ----- epilogue of this (point tile, MO tile)
         if (!(ok = warp_wait(s, K::B_ACCFULL, u & 1, a.err))) break;
         ptx::tc_fence_after();
-        // s.part is read by the setup warp's sink of the previous (tile, MO tile)
-        if (u > 0 && !(ok = warp_wait(s, K::B_EPIFREE, (u - 1) & 1, a.err))) break;
-        float *part = s.part + q * 320;
+        // partial-sum buffer u & 1 was read by the setup warp's sink of pass u - 2
+        const int pb = (int)(u & 1u);
+        if (u >= 2 && !(ok = warp_wait(s, K::B_EPIFREE + pb, ((u >> 1) - 1) & 1, a.err))) break;
+        float *part = s.part + pb * 1280 + q * 320;
         if (nact > 0) {
           const float occ = a.occ[mo];
 #pragma unroll 1
@@ -1289,7 +1296,7 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
         __syncwarp();
         if (lane == 0) {
           ptx::mbar_arrive(&s.bar[K::B_ACCEMPTY]);
-          ptx::mbar_arrive(&s.bar[K::B_EPIFULL]);
+          ptx::mbar_arrive(&s.bar[K::B_EPIFULL + pb]);
         }
       }
       __syncwarp();

@@ -411,7 +411,11 @@ typedef struct {
  * converged ones (cpeps 1e-2, nuceps 0.1, nucepsh 0.2, gradient check
  * max(1e-4, gfnormeps), degenerate CPs dropped), sortcps.  Outputs up to
  * maxcp CPs: cp_xyz(3,*), cp_typ(*) (signature: -3 n, -1 b, 1 r, 3 c),
- * cp_f(*) density.  With xseed NULL the default pair seeds are used. */
+ * cp_f(*) density.  With xseed NULL the default pair seeds are used, each
+ * unordered atom pair once: critic2 seeds both ordered pairs, whose points
+ * coincide (the k-th point of i->j is the (6-k)-th of j->i), so its list
+ * (c2g_pair_seeds) holds every seed twice; taking one of each gives the same
+ * CP list with half the Newton work. */
 int c2g_autocritic(c2g_wfn *h, int nseed, const double *xseed, int prec, int maxcp,
                    double *cp_xyz, int *cp_typ, double *cp_f, c2g_cp_report *report);
 

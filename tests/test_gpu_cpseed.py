@@ -223,19 +223,29 @@ def trained():
 
 
 def test_learned_autocritic_vs_plain(gpu_lib, trained):
-    """On held-out molecules of the training family: the learned search either
-    passes its check (Poincare-Hopf, or a CP set stable under a denser seed
-    set outside the nuclear cores) or falls back to the plain pair seeds and
-    then reproduces the plain search exactly; an untrained network (no
-    confident heat-map peaks) always falls back."""
+    """What the trained network gains, on held-out molecules of the training
+    family (FP64, critic2's Newton), against the method without it (seeds at
+    the minima of s on the same coarse grid) and against plain pair seeding:
+    its proposal recovers at least 95% of the plain search's CPs, at least 10
+    points more than the coarse-grid seeds, with fewer seeds than the plain
+    search (distinct atom pairs) and under half of critic2's own seed list
+    (ordered pairs: every midpoint twice), which finds the same CPs as the
+    plain search.  The checked search either passes its check or falls back
+    and then reproduces the plain search; an untrained network (no confident
+    heat-map peaks) always falls back."""
     from critic2_gb300 import cpseed
     untrained = cpseed.SeedNet(seed=11).rounded()
     for j in range(2):
         mol = synth.training_molecule(10 ** 6 + 100 + j, natom_range=(20, 40))
         st = cpseed.evaluate(mol, trained, "fp64")
-        print("\n" + str({k: st[k] for k in ("natom", "ncp", "recall", "recall_outside_cores", "stage",
-                                              "reason", "plain_seeds", "learned_seeds", "ms_plain",
-                                              "ms_learned")}))
+        prop, grid = st["proposal"], st["grid_seeds"]
+        print("\n" + str({k: st[k] for k in ("natom", "ncp", "recall", "stage", "plain_seeds", "ms_plain",
+                                              "ms_learned")}) + f" proposal {prop} grid seeds {grid}")
+        assert prop["recall"] >= 0.95
+        assert prop["recall"] >= grid["recall"] + 0.10
+        assert prop["seeds"] < st["plain_seeds"]
+        assert prop["seeds"] * 2 < st["critic2_seed_list"]["seeds"]
+        assert st["critic2_seed_list"]["same_cps"]
         if st["stage"] == "fallback":
             assert st["recall"] == 1.0
         else:

@@ -266,6 +266,23 @@ def test_autocritic_cp100_vs_oracle(gpu_lib, oracle_mod):
           f"{int(in_ref.sum())} common, GPU-only {len(only_g)}, oracle-only {len(only_o)}")
 
 
+def test_autocritic_distinct_pair_seeds(gpu_lib):
+    """The default seeding takes each unordered atom pair once; critic2's own
+    list (c2g_pair_seeds: both ordered pairs, every point twice) gives the
+    same CP list, types, densities and Poincare-Hopf sum (cp100)."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("cp100")
+    g = Wavefunction(mol)
+    full = g.pair_seeds()
+    a = g.autocritic(prec="fp64")
+    b = g.autocritic(full, prec="fp64")
+    assert a["nseed"] * 2 == len(full)
+    assert len(a["xyz"]) == len(b["xyz"]) and list(a["counts"]) == list(b["counts"]) and a["ph"] == b["ph"]
+    assert np.allclose(a["xyz"], b["xyz"], rtol=0, atol=1e-9)
+    assert np.array_equal(a["typ"], b["typ"])
+    assert np.allclose(a["f"], b["f"], rtol=1e-12, atol=0)
+
+
 def test_error_paths(pair12, gpu_lib):
     g, _ = pair12
     with pytest.raises(gpu_lib.C2GError) as e:
