@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libcritic2_gb300.so")
 
 C2G_OK = 0
 PREC = {"fp64": 0, "tf32x3": 1, "bf16x3": 2}
-ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported"}
+ERRORS = {1: "argument", 2: "cuda", 3: "alloc", 4: "io", 5: "unsupported", 6: "numeric"}
 
 # every symbol include/critic2_gb300.h declares
 EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_wfx", "c2g_wfn_read_wfn", "c2g_wfn_read_fchk", "c2g_wfn_read_molden",
@@ -23,7 +23,7 @@ EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_
            "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
            "c2g_autocritic", "c2g_nci_post_dev", "c2g_cube_text", "c2g_dat_text", "c2g_nciplot_files",
            "c2g_grid_field_dev", "c2g_cube_precise_text", "c2g_cube_field_file",
-           "c2g_nci_chk_write", "c2g_nci_chk_read", "c2g_cp_graph",
+           "c2g_nci_chk_write", "c2g_nci_chk_read", "c2g_cp_graph", "c2g_basin_size", "c2g_basin_integrals",
            "c2g_mesh_size", "c2g_mesh_dev", "c2g_molcalc",
            # learned CP-seed proposer (include/critic2_gb300_cpseed.h)
            "c2g_cs_conv3d", "c2g_cs_conv3d_bwd_data", "c2g_cs_conv3d_bwd_weight", "c2g_cs_loss",
@@ -48,6 +48,11 @@ class NciCut(C.Structure):
 
 class GraphStats(C.Structure):
     _fields_ = [("npath", C.c_int), ("nbatch", C.c_int), ("nevals", C.c_long), ("ms_total", C.c_double)]
+
+
+class BasinStats(C.Structure):
+    _fields_ = [("natt", C.c_int), ("nray", C.c_int), ("npath", C.c_long), ("nbatch", C.c_long),
+                ("nevals", C.c_long), ("nwarn", C.c_int), ("nrestart", C.c_int), ("ms_total", C.c_double)]
 
 
 class MeshStats(C.Structure):
@@ -89,6 +94,10 @@ def lib():
     L.c2g_mesh_dev.argtypes = [_vp, C.c_int, C.c_int, _vp, _vp, _vp]
     L.c2g_molcalc.argtypes = [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, C.POINTER(MeshStats)]
     L.c2g_cp_graph.argtypes = [_vp, C.c_int, _vp, _vp] + [_vp] * 7 + [C.POINTER(GraphStats)]
+    L.c2g_basin_size.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int)]
+    L.c2g_basin_integrals.argtypes = [_vp, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double] + \
+        [_vp] * 6 + [C.POINTER(BasinStats)]
     L.c2g_nci_chk_write.argtypes = [C.c_char_p, _dp, _dp, _ip, _dp, _dp]
     L.c2g_nci_chk_read.argtypes = [C.c_char_p, _dp, _dp, _ip, _dp, _dp, C.POINTER(C.c_int)]
     L.c2g_wfn_info.argtypes = [_vp] + [C.POINTER(C.c_int)] * 5

@@ -153,6 +153,12 @@ void launch_fp64_nci_grid(const DevWfn &w, const GridSpec &g, double *d_crho, do
 void launch_fp64_nci_list(const DevWfn &w, const GridSpec &g, const int *d_list, const int *d_count,
                           int maxn, double *d_crho, double *d_cgrad, cudaStream_t st);
 
+// mesh.cu: the n-point Lebedev rule (x, y, z, weight summing to 1; the
+// sizes of good_lebedev, 6 to 5810) and Gauss-Legendre nodes and weights on
+// (a, b), ascending (gauleg, src/tools_math@proc.f90:1765-1826).
+std::vector<double4> lebedev_points(int n);
+void gauleg(double a, double b, int n, std::vector<double> &x, std::vector<double> &w);
+
 // k_newton.cu: batched field%newton on device arrays x(3,n), ier(n)
 void newton_batch_dev(Handle &h, int n, double *d_x, int *d_ier, double gfnormeps, int maxit,
                       int prec, cudaStream_t st);

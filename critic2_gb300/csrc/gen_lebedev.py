@@ -1,6 +1,7 @@
-"""Writes lebedev_tables.h: the Lebedev-Laikov angular quadratures of 110,
-194, 302, 590 and 770 points (degrees 17, 23, 29, 41, 47; the sizes
-critic2's molecular meshes use) as octahedral orbit representatives.
+"""Writes lebedev_tables.h: the Lebedev-Laikov angular quadratures of every
+size critic2's good_lebedev offers (6 to 5810 points, degrees 3 to 131:
+the molecular meshes use 110-770, the basin integrals any of them) as
+octahedral orbit representatives.
 
 The rules are taken from scipy.integrate.lebedev_rule (scipy >= 1.15,
 which tabulates Lebedev and Laikov's published parameters).  Each orbit is
@@ -13,7 +14,10 @@ import itertools
 import numpy as np
 from scipy.integrate import lebedev_rule
 
-RULES = ((110, 17), (194, 23), (302, 29), (590, 41), (770, 47))
+RULES = ((6, 3), (14, 5), (26, 7), (38, 9), (50, 11), (74, 13), (86, 15), (110, 17), (146, 19), (170, 21),
+         (194, 23), (230, 25), (266, 27), (302, 29), (350, 31), (434, 35), (590, 41), (770, 47), (974, 53),
+         (1202, 59), (1454, 65), (1730, 71), (2030, 77), (2354, 83), (2702, 89), (3074, 95), (3470, 101),
+         (3890, 107), (4334, 113), (4802, 119), (5294, 125), (5810, 131))
 
 
 def orbits(n, deg):

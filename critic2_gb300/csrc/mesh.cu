@@ -489,3 +489,15 @@ int c2g_molcalc(c2g_wfn *hp, int type, int level, int prec, int nq, const int *q
 }
 
 }  // extern "C"
+
+namespace c2g {
+
+std::vector<double4> lebedev_points(int n) { return lebedev(n); }
+
+void gauleg(double a, double b, int n, std::vector<double> &x, std::vector<double> &w) {
+  gauss_legendre(n, x, w);
+  const double xm = 0.5 * (b + a), xl = 0.5 * (b - a);
+  for (int i = 0; i < n; i++) x[i] = xm + xl * x[i], w[i] *= xl;
+}
+
+}  // namespace c2g

@@ -286,6 +286,34 @@ class Wavefunction:
         o["stats"] = dict(npath=st.npath, nbatch=st.nbatch, nevals=st.nevals, ms=st.ms_total)
         return o
 
+    def basin_integrals(self, cp_xyz=None, cp_typ=None, meth: str = "lebedev", n: int = 110, nphi: int = 0,
+                        cpid: int = 0, iasprec: float = 1e-5) -> dict:
+        """Atomic-basin integrals by bisection (c2g_basin_integrals; critic2's
+        INTEGRALS LEBEDEV n / GAULEG n nphi [CP cpid]).  The CP list is
+        c2g_autocritic's (nuclei first); None for the nuclei alone.  Returns
+        att_cp (natt,), props (natt, 2: Pop, Lap), iaserr (natt, 2),
+        rays (nray, 3), rsurf (natt, nray), rbeta_int (natt,), stats."""
+        if cp_xyz is None:
+            x, t, ncp = None, None, 0
+        else:
+            x, t = _f64(cp_xyz).reshape(-1, 3), _i32(cp_typ)
+            ncp = t.shape[0]
+        m = {"lebedev": 0, "gauleg": 1}[meth]
+        natt, nray = C.c_int(0), C.c_int(0)
+        L.check(L.lib().c2g_basin_size(self._h, ncp, L.ptr(t) if t is not None else None, m, int(n), int(nphi),
+                                       int(cpid), C.byref(natt), C.byref(nray)))
+        na, nr = natt.value, nray.value
+        o = dict(att_cp=np.zeros(na, np.int32), props=np.zeros((na, 2)), iaserr=np.zeros((na, 2)),
+                 rays=np.zeros((nr, 3)), rsurf=np.zeros((na, nr)), rbeta_int=np.zeros(na))
+        st = L.BasinStats()
+        L.check(L.lib().c2g_basin_integrals(
+            self._h, ncp, L.ptr(x) if x is not None else None, L.ptr(t) if t is not None else None, m, int(n),
+            int(nphi), int(cpid), float(iasprec), L.ptr(o["att_cp"]), L.ptr(o["props"]), L.ptr(o["iaserr"]),
+            L.ptr(o["rays"]), L.ptr(o["rsurf"]), L.ptr(o["rbeta_int"]), C.byref(st)))
+        o["stats"] = dict(natt=st.natt, nray=st.nray, npath=st.npath, nbatch=st.nbatch, nevals=st.nevals,
+                          nwarn=st.nwarn, nrestart=st.nrestart, ms=st.ms_total)
+        return o
+
     def autocritic(self, seeds: Optional[np.ndarray] = None, prec="fp64") -> dict:
         s = None if seeds is None else _f64(seeds).reshape(-1, 3)
         ns = 0 if s is None else s.shape[0]

@@ -48,6 +48,7 @@ extern "C" {
 #define C2G_ERR_ALLOC 3       /* host or device allocation failed */
 #define C2G_ERR_IO 4          /* file could not be read or parsed */
 #define C2G_ERR_UNSUPPORTED 5 /* valid request this build does not support */
+#define C2G_ERR_NUMERIC 6     /* the algorithm cannot complete on this input (critic2 stops there too) */
 
 /* arithmetic of the evaluation */
 #define C2G_PREC_FP64 0   /* FP64 everywhere (the plain form) */
@@ -452,6 +453,62 @@ typedef struct {
 
 int c2g_cp_graph(c2g_wfn *h, int ncp, const double *cp_xyz, const int *cp_typ, int *ipath, double *brdist,
                  double *brpathlen, double *brang, double *brvec, int *ier, int *nstep, c2g_graph_stats *stats);
+
+/* Atomic-basin integrals by bisection of the zero-flux surface: critic2's
+ * INTEGRALS keyword for a molecular wavefunction field
+ * (src/bisect@proc.f90:862-1028; INTEGRALS LEBEDEV n / GAULEG ntheta nphi,
+ * CP id).  The attractors are the nuclei and the CPs of type -3 of the CP
+ * list (cpid = 0), or the one CP cpid (1-based).  For each attractor and
+ * angular node the surface radius is found as bisect_msurface does
+ * (:1208-1446): a bracket from critic2's tries at 2e-5 bohr, 0.9 and 0.99
+ * of the distance to the nearest CP (inner; the largest whose upward
+ * gradient path ends within sqrt(1e-5) bohr of the attractor) and the cell
+ * size, 0.75 and 0.99 of the distance to the nearest CP of the same type
+ * (outer; the smallest whose path does not), then bisection to iasprec
+ * bohr (lim_surf, :1039-1126; critic2's default INT_iasprec 1e-5), with
+ * field%gradient's navigation and beta spheres of 0.1 bohr shrunk by 0.75
+ * when a surface point falls inside one.  The integral is a beta sphere of
+ * 0.95 times the smallest surface radius (170-point Lebedev rule) plus the
+ * radial Gauss-Legendre quadrature (50 nodes) of each ray from the sphere to
+ * the surface, summed as lebedev_mquad / gauleg_mquad
+ * (src/integration@proc.f90:495-642).  Integrated properties are critic2's
+ * molecular defaults: the valence density (Pop) and its Laplacian (Lap).
+ *   meth C2G_INT_LEBEDEV: n1 = rule size (rounded up to the next of
+ *        critic2's 32 sizes, 6-5810); C2G_INT_GAULEG: n1 = ntheta,
+ *        n2 = nphi (int(nphi |sin theta|) + 1 nodes per polar ring).
+ *   CP list: c2g_autocritic's (the nuclei first, in atom order), or ncp = 0
+ *        for the nuclei alone.
+ * Outputs (natt and nray from c2g_basin_size):
+ *   att_cp(natt)          0-based CP index of each attractor (may be NULL)
+ *   props(2, natt)        Pop, Lap per attractor
+ *   iaserr(2, natt)       critic2's IAS error estimate (may be NULL)
+ *   rays(3, nray)         unit direction of each node (may be NULL)
+ *   rsurf(nray, natt)     surface radius per attractor and node (may be NULL)
+ *   rbeta_int(natt)       beta-sphere radius (may be NULL)
+ * Rays are independent: unlike a serial critic2 run, a ray's bracket does
+ * not depend on running means over the rays done before it (every ray
+ * takes the first ray's tries), so end points can differ from critic2's by
+ * up to iasprec; and a beta sphere shrunk by a ray's restart stays shrunk for
+ * that ray only.  A ray without a bracket returns C2G_ERR_NUMERIC (critic2:
+ * "Can not find ray limits"). */
+#define C2G_INT_LEBEDEV 0
+#define C2G_INT_GAULEG 1
+typedef struct {
+  int natt;        /* attractors integrated */
+  int nray;        /* rays per attractor */
+  long npath;      /* gradient paths traced */
+  long nbatch;     /* GPU evaluation batches of the surface search */
+  long nevals;     /* field evaluations (paths and quadrature) */
+  int nwarn;       /* paths that ended with field%gradient's ier > 0 */
+  int nrestart;    /* beta-sphere shrinks (bisection restarts) */
+  double ms_total; /* wall time of the call */
+} c2g_basin_stats;
+
+int c2g_basin_size(c2g_wfn *h, int ncp, const int *cp_typ, int meth, int n1, int n2, int cpid, int *natt,
+                   int *nray);
+int c2g_basin_integrals(c2g_wfn *h, int ncp, const double *cp_xyz, const int *cp_typ, int meth, int n1, int n2,
+                        int cpid, double iasprec, int *att_cp, double *props, double *iaserr, double *rays,
+                        double *rsurf, double *rbeta_int, c2g_basin_stats *stats);
 
 #ifdef __cplusplus
 }

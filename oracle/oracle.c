@@ -7,6 +7,7 @@
  */
 #include "oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -973,8 +974,19 @@ static int adaptive_stepper(const owfn *w, double x[3], double *h0, double maxst
  * (going down, ier 3), when it bounces (5 reversals) or the step falls
  * under 1e-12 (ier 1), or after nint(1000/0.3) steps (ier 2).  x: start
  * (in) and end point (out); plen starts at |x - pathini|. */
+static int o_gradient_rb(const owfn *w, double x[3], int iup, int ncp, const double *cpx, const int *cptyp,
+                         const double *rbeta, const double pathini[3], int *nstep_out, double *plen_out);
+
 int o_gradient(const owfn *w, double x[3], int iup, int ncp, const double *cpx, const int *cptyp,
                const double pathini[3], int *nstep_out, double *plen_out) {
+  return o_gradient_rb(w, x, iup, ncp, cpx, cptyp, NULL, pathini, nstep_out, plen_out);
+}
+
+/* The same with up2beta and per-CP beta radii rbeta (the CP list starting
+ * with the nuclei in atom order, so that a nucleus found first is CP
+ * idnuc); rbeta NULL: the default sphere min(Rbetadef, |hini|/2) = 0.1. */
+static int o_gradient_rb(const owfn *w, double x[3], int iup, int ncp, const double *cpx, const int *cptyp,
+                         const double *rbeta, const double pathini[3], int *nstep_out, double *plen_out) {
   const double minstep = 1e-12, hfirst = 0.01;
   const int mhist = 5;
   double hini = NAV_STEP * iup, h0 = hfirst * iup;
@@ -1011,7 +1023,7 @@ int o_gradient(const owfn *w, double x[3], int iup, int ncp, const double *cpx, 
         for (int j = 0; j < 3; j++) xcp[j] = cpx[3 * i + j];
       }
     }
-    if (idcp >= 0 && cprad <= RBETADEF) {
+    if (idcp >= 0 && cprad <= (rbeta ? rbeta[idcp] : RBETADEF)) {
       incstep = 1;
       double e2 = 0.0;
       for (int j = 0; j < 3; j++) e2 += (x[j] - xcp[j]) * (x[j] - xcp[j]);
@@ -1371,4 +1383,287 @@ void o_fmt_E22_14E3(double x, char *out) {
   dig[14] = 0;
   snprintf(t, sizeof t, "%c0.%sE%c%03d", neg ? '-' : ' ', dig, e < 0 ? '-' : '+', e < 0 ? -e : e);
   memcpy(out, t, 22);
+}
+
+/* ------------------------------------------------------------------ */
+/* Atomic-basin integrals by bisection (critic2's INTEGRALS for a molecule,
+ * src/bisect@proc.f90:862-1028), the surface search of bisect_msurface
+ * (:1208-1446) and lim_surf (:1039-1126), the radial quadrature of
+ * int_radialquad (src/integration@proc.f90:384-486, Gauss-Legendre, 50
+ * nodes) and the angular sums of lebedev_mquad / gauleg_mquad (:495-642),
+ * with a 170-point Lebedev beta sphere (sphereintegrals_lebedev,
+ * src/bisect@proc.f90:829-854).  Integrated: the valence density and its
+ * Laplacian (grdall's fval and del2fval for critic2's molecular default
+ * properties Pop and Lap). */
+
+#define BS_RNEARNUC 3.1622776601683794e-3 /* sqrt(1e-5), src/bisect@proc.f90:50 */
+#define BS_NTRIES 7
+#define BS_NRAD 50
+
+typedef struct {
+  int idone;
+  double rnearsum, rfarsum, rzfssum, rnearmin, rfarmax;
+} o_bstats;
+
+static int cmp_dbl(const void *a, const void *b) {
+  double x = *(const double *)a, y = *(const double *)b;
+  return (x > y) - (x < y);
+}
+
+static double dist3(const double *a, const double *b) {
+  double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+  return sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+}
+
+/* up-path from x; returns ier, end point in x */
+static int o_uppath(const owfn *w, double x[3], int ncp, const double *cpx, const int *cptyp, const double *rbeta) {
+  int nstep;
+  double plen;
+  return o_gradient_rb(w, x, 1, ncp, cpx, cptyp, rbeta, x, &nstep, &plen);
+}
+
+/* lim_surf: bisection between xin and xfin to within delta; restarts with
+ * a smaller beta sphere when the result lies in one of the attractor's
+ * type.  Returns the surface point in xmed. */
+static void o_lim_surf(const owfn *w, int ncp, const double *cpx, const int *cptyp, double *rbeta, const double *xnuc,
+                       int typ, const double xin[3], const double xfin[3], double delta, double xmed[3], int *nwarn,
+                       int *nrestart) {
+  for (;;) {
+    double xi[3], xf[3];
+    for (int j = 0; j < 3; j++) xi[j] = xin[j], xf[j] = xfin[j];
+    while (dist3(xi, xf) > delta) {
+      double xp[3];
+      for (int j = 0; j < 3; j++) xmed[j] = xp[j] = 0.5 * (xi[j] + xf[j]);
+      int ier = o_uppath(w, xp, ncp, cpx, cptyp, rbeta), inside;
+      if (ier <= 0) {
+        inside = dist3(xp, xnuc) <= BS_RNEARNUC;
+      } else if (ier == 3) {
+        inside = 0;
+      } else {
+        double best = 1e300;
+        (*nwarn)++;
+        for (int i = 0; i < ncp; i++)
+          if (cptyp[i] == -3) best = fmin(best, dist3(cpx + 3 * i, xp));
+        inside = best <= BS_RNEARNUC;
+      }
+      for (int j = 0; j < 3; j++) {
+        if (inside) xi[j] = xmed[j];
+        else xf[j] = xmed[j];
+      }
+    }
+    for (int j = 0; j < 3; j++) xmed[j] = 0.5 * (xi[j] + xf[j]);
+    int again = 0;
+    for (int i = 0; i < ncp && !again; i++) {
+      if (cptyp[i] != typ) continue;
+      if (dist3(cpx + 3 * i, xmed) <= rbeta[i]) {
+        rbeta[i] *= 0.75;
+        (*nrestart)++;
+        again = 1;
+      }
+    }
+    if (!again) return;
+  }
+}
+
+/* bisect_msurface for one ray u of the attractor at xcar; st NULL: every
+ * ray takes the first ray's bracket tries.  Returns the surface radius, or
+ * -1 when no bracket is found ("Can not find ray limits"). */
+static double o_bisect_ray(const owfn *w, int ncp, const double *cpx, const int *cptyp, double *rbeta,
+                           const double *xcar, int typ, double rmin, double rminsame, const double u[3], double prec,
+                           o_bstats *st, int *nwarn, int *nrestart) {
+  const double vbig = DBL_MAX;
+  double amin = fmin(w->aa[0], fmin(w->aa[1], w->aa[2])), amax = fmax(w->aa[0], fmax(w->aa[1], w->aa[2]));
+  int idone = st ? st->idone : 0;
+  double rtry[BS_NTRIES], x[3];
+  double rother = vbig, raprox = vbig, riaprox = 0.0;
+  rtry[0] = 2e-5, rtry[1] = 0.9 * rmin, rtry[2] = 0.99 * rmin;
+  if (idone > 0) {
+    rtry[3] = 0.99 * st->rnearmin, rtry[4] = st->rnearsum / idone, rtry[5] = 0.8 * st->rzfssum / idone, rtry[6] = 0.0;
+  } else {
+    rtry[3] = rtry[4] = rtry[5] = rtry[6] = 0.0;
+  }
+  qsort(rtry, BS_NTRIES, sizeof(double), cmp_dbl);
+  for (int k = BS_NTRIES - 1; k >= 0; k--) {
+    riaprox = rtry[k];
+    for (int j = 0; j < 3; j++) x[j] = xcar[j] + riaprox * u[j];
+    int ier = o_uppath(w, x, ncp, cpx, cptyp, rbeta);
+    if (ier == 3) {
+      if (rtry[k] < rother) rother = rtry[k];
+    } else {
+      if (ier > 0) (*nwarn)++;
+      if (dist3(x, xcar) <= BS_RNEARNUC) break;
+      if (rtry[k] < rother) rother = rtry[k];
+    }
+  }
+  rtry[0] = amin, rtry[1] = 0.99 * rminsame, rtry[2] = 0.75 * rminsame;
+  if (idone > 0) {
+    rtry[3] = 1.01 * st->rfarmax, rtry[4] = st->rfarsum / idone, rtry[5] = 1.2 * st->rzfssum / idone, rtry[6] = amax;
+  } else {
+    rtry[3] = rtry[4] = rtry[5] = rtry[6] = amax;
+  }
+  qsort(rtry, BS_NTRIES, sizeof(double), cmp_dbl);
+  raprox = rother;
+  for (int k = 0; k < BS_NTRIES; k++) {
+    raprox = rtry[k];
+    if (raprox > (rother + riaprox) / 2.0 || raprox < riaprox) {
+      raprox = rother;
+      continue;
+    }
+    for (int j = 0; j < 3; j++) x[j] = xcar[j] + raprox * u[j];
+    int ier = o_uppath(w, x, ncp, cpx, cptyp, rbeta);
+    if (ier == 3) {
+      if (raprox > riaprox) riaprox = raprox;
+      raprox = rother;
+    } else {
+      if (ier > 0) (*nwarn)++;
+      if (dist3(x, xcar) > BS_RNEARNUC) break;
+      if (raprox > riaprox) riaprox = raprox;
+      raprox = rother;
+    }
+  }
+  if (raprox == vbig || riaprox == 0.0) return -1.0;
+  double xin[3], xfin[3], xmed[3];
+  for (int j = 0; j < 3; j++) xin[j] = xcar[j] + riaprox * u[j], xfin[j] = xcar[j] + raprox * u[j];
+  o_lim_surf(w, ncp, cpx, cptyp, rbeta, xcar, typ, xin, xfin, prec, xmed, nwarn, nrestart);
+  double rlim = dist3(xmed, xcar);
+  if (st) {
+    st->rnearsum += riaprox, st->rfarsum += raprox, st->rzfssum += rlim;
+    st->rnearmin = fmin(st->rnearmin, riaprox), st->rfarmax = fmax(st->rfarmax, raprox);
+    st->idone++;
+  }
+  return rlim;
+}
+
+/* gauleg on (a, b), ascending */
+static void o_gauleg_ab(double a, double b, int n, double *x, double *wt) {
+  o_gauleg(n, x, wt);
+  double xm = 0.5 * (b + a), xl = 0.5 * (b - a);
+  for (int i = 0; i < n; i++) x[i] = xm + xl * x[i], wt[i] *= xl;
+}
+
+/* int_radialquad with Gauss-Legendre: integral of r^2 (fval, del2fval)
+ * from r0 to rend along u; iaserr from the end point */
+static void o_radialquad(const owfn *w, const double *x0, const double u[3], double r0, double rend, double prec,
+                         double lp[2], double ie[2]) {
+  double rr[BS_NRAD], rw[BS_NRAD], r1 = r0, r2 = rend, sg = 1.0;
+  if (rend <= r0) r1 = rend, r2 = r0, sg = -1.0;
+  o_gauleg_ab(r1, r2, BS_NRAD, rr, rw);
+  lp[0] = lp[1] = 0.0;
+  for (int k = 0; k < BS_NRAD; k++) {
+    double x[3];
+    ores res;
+    for (int j = 0; j < 3; j++) x[j] = x0[j] + rr[k] * u[j];
+    o_grd(w, x, 2, &res);
+    lp[0] += rr[k] * rr[k] * rw[k] * res.fval;
+    lp[1] += rr[k] * rr[k] * rw[k] * res.del2fval;
+  }
+  lp[0] *= sg, lp[1] *= sg;
+  if (ie) {
+    double x[3];
+    ores res;
+    for (int j = 0; j < 3; j++) x[j] = x0[j] + rend * u[j];
+    o_grd(w, x, 2, &res);
+    ie[0] = fabs(res.fval * rend * rend * prec);
+    ie[1] = fabs(res.del2fval * rend * rend * prec);
+  }
+}
+
+/* INTEGRALS for the attractors of the CP list (the nuclei, which it must
+ * start with in atom order, and the CPs of type -3; cpid > 0: that CP
+ * alone, 1-based).  Rays: unit vectors u(3, nray) with angular weights
+ * wang; ring NULL sums them as lebedev_mquad (weights times 4 pi), else
+ * ray i belongs to polar ring ring[i] whose factor sin(theta) w_theta is
+ * ringw[ring[i]] and wang is the azimuthal weight (gauleg_mquad).  The beta
+ * sphere uses usph/wsph (nsph points, weights times 4 pi).  stats: critic2's
+ * running bracket statistics over the rays in order and beta radii shared
+ * by all rays and attractors (serial, as critic2 with one thread); else
+ * every ray takes the first ray's tries and shrinks its own copy of the
+ * beta radii (rays in parallel).  Outputs per
+ * attractor a: props(2, natt) Pop, Lap; iaserr(2, natt); rsurf(nray, natt);
+ * rbeta_int(natt); att_cp(natt).  Returns the attractor count, or -1 when
+ * a ray has no bracket. */
+int o_basin_integrals(const owfn *w, int ncp, const double *cpx, const int *cptyp, int cpid, int nray,
+                      const double *u, const double *wang, const int *ring, int nring, const double *ringw, int nsph,
+                      const double *usph, const double *wsph, double prec, int stats, int nthreads, int *att_cp,
+                      double *props, double *iaserr, double *rsurf, double *rbeta_int, int *nwarn_out,
+                      int *nrestart_out) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  int lo = cpid > 0 ? cpid - 1 : 0, hi = cpid > 0 ? cpid : ncp, natt = 0, fail = 0, nwarn = 0, nrestart = 0;
+  double *rbeta = malloc(sizeof(double) * (ncp > 0 ? ncp : 1));
+  for (int i = 0; i < ncp; i++) rbeta[i] = RBETADEF;
+  for (int c = lo; c < hi; c++) {
+    if (!(c < w->natom || cptyp[c] == -3)) continue;
+    const double *xcar = cpx + 3 * c;
+    double rmin = DBL_MAX, rminsame = DBL_MAX;
+    for (int i = 0; i < ncp; i++) {
+      double d = dist3(cpx + 3 * i, xcar);
+      if (d < 1e-5) continue;
+      rmin = fmin(rmin, d);
+      if (cptyp[i] == cptyp[c]) rminsame = fmin(rminsame, d);
+    }
+    double *r = rsurf + (size_t)natt * nray;
+    if (stats) {
+      o_bstats st = {0, 0.0, 0.0, 0.0, DBL_MAX, 0.0};
+      for (int i = 0; i < nray && !fail; i++) {
+        r[i] = o_bisect_ray(w, ncp, cpx, cptyp, rbeta, xcar, cptyp[c], rmin, rminsame, u + 3 * i, prec, &st, &nwarn,
+                            &nrestart);
+        if (r[i] < 0) fail = 1;
+      }
+    } else {
+      /* every ray on its own copy of the beta radii */
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : nwarn, nrestart)
+      for (int i = 0; i < nray; i++) {
+        double *rb = malloc(sizeof(double) * (ncp > 0 ? ncp : 1));
+        for (int k = 0; k < ncp; k++) rb[k] = RBETADEF;
+        r[i] = o_bisect_ray(w, ncp, cpx, cptyp, rb, xcar, cptyp[c], rmin, rminsame, u + 3 * i, prec, NULL, &nwarn,
+                            &nrestart);
+        free(rb);
+      }
+      for (int i = 0; i < nray; i++)
+        if (r[i] < 0) fail = 1;
+    }
+    if (fail) break;
+    double rmn = DBL_MAX;
+    for (int i = 0; i < nray; i++) rmn = fmin(rmn, r[i]);
+    double rb = 0.95 * rmn;
+    /* the beta sphere */
+    double sp[2] = {0, 0};
+    for (int i = 0; i < nsph; i++) {
+      double lp[2];
+      o_radialquad(w, xcar, usph + 3 * i, 0.0, rb, prec, lp, NULL);
+      sp[0] += lp[0] * wsph[i], sp[1] += lp[1] * wsph[i];
+    }
+    /* the rays */
+    double *rp = malloc(sizeof(double) * 4 * (size_t)nray);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < nray; i++) o_radialquad(w, xcar, u + 3 * i, rb, r[i], prec, rp + 4 * i, rp + 4 * i + 2);
+    double lp[2] = {0, 0}, ie[2] = {0, 0};
+    if (!ring) {
+      for (int i = 0; i < nray; i++)
+        for (int q = 0; q < 2; q++) lp[q] += rp[4 * i + q] * wang[i], ie[q] += rp[4 * i + 2 + q] * wang[i];
+    } else {
+      for (int t = 0; t < nring; t++) {
+        double pr[2] = {0, 0}, pe[2] = {0, 0};
+        for (int i = 0; i < nray; i++) {
+          if (ring[i] != t) continue;
+          for (int q = 0; q < 2; q++) pr[q] += rp[4 * i + q] * wang[i], pe[q] += rp[4 * i + 2 + q] * wang[i];
+        }
+        for (int q = 0; q < 2; q++) lp[q] += ringw[t] * pr[q], ie[q] += ringw[t] * pe[q];
+      }
+    }
+    free(rp);
+    for (int q = 0; q < 2; q++) {
+      props[2 * natt + q] = lp[q] + sp[q];
+      iaserr[2 * natt + q] = ie[q];
+    }
+    rbeta_int[natt] = rb;
+    att_cp[natt] = c;
+    natt++;
+  }
+  free(rbeta);
+  if (nwarn_out) *nwarn_out = nwarn;
+  if (nrestart_out) *nrestart_out = nrestart;
+  return fail ? -1 : natt;
 }

@@ -99,6 +99,11 @@ int o_gradient(const owfn *w, double x[3], int iup, int ncp, const double *cpx, 
                const double pathini[3], int *nstep, double *plen);
 void o_makegraph(const owfn *w, int ncp, const double *cpx, const int *cptyp, int *ipath, double *brdist,
                  double *brpathlen, double *brang, double *brvec, int *ier, int *nstep, int nthreads);
+int o_basin_integrals(const owfn *w, int ncp, const double *cpx, const int *cptyp, int cpid, int nray,
+                      const double *u, const double *wang, const int *ring, int nring, const double *ringw, int nsph,
+                      const double *usph, const double *wsph, double prec, int stats, int nthreads, int *att_cp,
+                      double *props, double *iaserr, double *rsurf, double *rbeta_int, int *nwarn_out,
+                      int *nrestart_out);
 
 /* Molecular meshes (src/meshmod@proc.f90:79-627): type 1 Becke, 2
  * Franchini; ang(4, nang) the angular rule (weights sum to 1). */

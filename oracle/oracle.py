@@ -77,6 +77,10 @@ def lib():
                                  C.POINTER(C.c_double)]
         L.o_gradient.restype = C.c_int
         L.o_makegraph.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, C.c_int]
+        L.o_basin_integrals.argtypes = [C.c_void_p, C.c_int, _dp, _ip, C.c_int, C.c_int, _dp, _dp, C.c_void_p,
+                                        C.c_int, C.c_void_p, C.c_int, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                        _ip, _dp, _dp, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.o_basin_integrals.restype = C.c_int
         L.o_z2nr.argtypes = [C.c_int, C.c_int]
         L.o_z2nr.restype = C.c_int
         L.o_mesh_size.argtypes = [C.c_void_p, C.c_int, C.c_int]
@@ -207,6 +211,37 @@ class Wfn:
         lib().o_makegraph(self.h, n, _f64(cp_xyz).reshape(-1), ct, out["ipath"].reshape(-1),
                           out["brdist"].reshape(-1), out["brpathlen"].reshape(-1), out["brang"],
                           out["brvec"].reshape(-1), out["ier"].reshape(-1), out["nstep"].reshape(-1), nthreads)
+        return out
+
+    def basin_integrals(self, cp_xyz, cp_typ, u, wang, usph, wsph, ring=None, ringw=None, cpid=0, prec=1e-5,
+                        stats=False, nthreads=0):
+        """INTEGRALS by bisection (molecule): rays u (nray, 3) with angular
+        weights wang (times 4 pi for a Lebedev rule; with ring/ringw the
+        gauleg_mquad grouping), beta sphere on usph/wsph.  stats: critic2's
+        serial running bracket statistics.  Returns a dict of att_cp,
+        props (natt, 2: Pop, Lap), iaserr, rsurf (natt, nray), rbeta_int,
+        nwarn, nrestart; raises RuntimeError when a ray has no bracket."""
+        ct = _i32(cp_typ)
+        n = len(ct)
+        nat = self.mol.natom
+        cand = [i for i in (range(n) if cpid <= 0 else [cpid - 1]) if i < nat or ct[i] == -3]
+        na, nray = len(cand), len(u)
+        out = dict(att_cp=np.zeros(max(na, 1), np.int32), props=np.zeros((max(na, 1), 2)),
+                   iaserr=np.zeros((max(na, 1), 2)), rsurf=np.zeros((max(na, 1), nray)), rbeta_int=np.zeros(max(na, 1)))
+        nw, nr = C.c_int(0), C.c_int(0)
+        rg = _i32(ring) if ring is not None else None
+        rw = _f64(ringw) if ringw is not None else None
+        got = lib().o_basin_integrals(
+            self.h, n, _f64(cp_xyz).reshape(-1), ct, int(cpid), nray, _f64(u).reshape(-1), _f64(wang),
+            rg.ctypes.data_as(C.c_void_p) if rg is not None else None, len(rw) if rw is not None else 0,
+            rw.ctypes.data_as(C.c_void_p) if rw is not None else None, len(usph), _f64(usph).reshape(-1),
+            _f64(wsph), float(prec), int(bool(stats)), int(nthreads), out["att_cp"], out["props"].reshape(-1),
+            out["iaserr"].reshape(-1), out["rsurf"].reshape(-1), out["rbeta_int"], C.byref(nw), C.byref(nr))
+        if got < 0:
+            raise RuntimeError("basin bisection: can not find ray limits")
+        for k in ("att_cp", "props", "iaserr", "rsurf", "rbeta_int"):
+            out[k] = out[k][:got]
+        out["nwarn"], out["nrestart"] = nw.value, nr.value
         return out
 
     def mesh(self, mesh="franchini", level="good", nthreads=0):
