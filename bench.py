@@ -53,6 +53,14 @@ EXTRA = ("prec200", "nci60")
 # ncu captures summarised under profiles/ (traffic grows with the points; the
 # coefficient operands stay in L2).
 TRAFFIC_PER_POINT = {}
+BASIN_NLEB = 26  # angular rule of the basin-integral part
+
+
+def lebedev_dirs(rule):
+    """Ray directions rebuilt from (theta, phi) as critic2's lebedev_nodes
+    does, and the weights times 4 pi."""
+    th, ph = np.arccos(rule[:, 2]), np.arctan2(rule[:, 1], rule[:, 0])
+    return np.c_[np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], rule[:, 3] * 4 * np.pi
 
 # Dense TF32 tensor rate of this GPU model measured with a cuBLAS TF32 GEMM
 # (TFLOP/s), a cross-check of the peak used below (half the measured BF16
@@ -219,6 +227,19 @@ def run_reference(args, wl, mol):
         line["molcalc"] = {"workload": "nci60", "mesh": "franchini, good", "quantity": "integral of rho",
                            "unit": "ms", "ms": 1e3 * (time.perf_counter() - t0), "integral": r["rho"],
                            "npoints": r["npoints"], "cores": threads, "kind": "port"}
+    if not args.no_basin:
+        # basin integrals by bisection on nci60 (the nuclei as attractors),
+        # Lebedev 26, all host threads
+        bmol = synth.make_molecule("nci60")
+        ob = oracle.Wfn(bmol)
+        u, wu = lebedev_dirs(oracle.lebedev_rule(BASIN_NLEB))
+        us, ws = lebedev_dirs(oracle.lebedev_rule(170))
+        t0 = time.perf_counter()
+        r = ob.basin_integrals(bmol.atom_xyz, np.full(bmol.natom, -3, np.int32), u, wu, us, ws, nthreads=threads)
+        line["basin"] = {"workload": f"nci60: INTEGRALS LEBEDEV {BASIN_NLEB}, nuclei", "unit": "ms",
+                         "ms": 1e3 * (time.perf_counter() - t0), "natt": int(len(r["att_cp"])),
+                         "nray": int(len(u)), "pop_sum": float(r["props"][:, 0].sum()), "cores": threads,
+                         "kind": "port"}
     if not args.no_cp:
         # the metric's second part on the CPU: AUTO with critic2's pair seeds
         # on the 100-atom molecule, all host threads
@@ -428,6 +449,7 @@ def main():
     ap.add_argument("--no-cp", action="store_true", help="skip the CP-search part")
     ap.add_argument("--no-files", action="store_true", help="skip the cube/dat output part")
     ap.add_argument("--no-mesh", action="store_true", help="skip the molcalc mesh-integral part")
+    ap.add_argument("--no-basin", action="store_true", help="skip the basin-integral part")
     ap.add_argument("--no-extra", action="store_true", help="skip the other workloads")
     ap.add_argument("--fp64-planes", type=int, default=-1,
                     help="FP64 comparison on this many i-planes spread over the grid (0: the whole grid; "
@@ -541,6 +563,18 @@ def main():
             mc[p_] = {"ms": 1e3 * (time.perf_counter() - t0), "integral": r["rho"], "ms_mesh": r["ms_mesh"]}
             mc["npoints"] = r["npoints"]
         line["molcalc"] = mc
+    if rank == 0 and not args.no_basin:
+        # basin integrals by bisection (critic2's INTEGRALS LEBEDEV n) on
+        # nci60, the nuclei as attractors: surfaces traced on the GPU
+        w3 = Wavefunction(synth.make_molecule("nci60"))
+        w3.basin_integrals(None, None, "lebedev", 6, cpid=1)  # warm-up
+        t0 = time.perf_counter()
+        r = w3.basin_integrals(None, None, "lebedev", BASIN_NLEB)
+        st = r["stats"]
+        line["basin"] = {"workload": f"nci60: INTEGRALS LEBEDEV {BASIN_NLEB}, nuclei", "unit": "ms",
+                         "ms": 1e3 * (time.perf_counter() - t0), "natt": st["natt"], "nray": st["nray"],
+                         "pop_sum": float(r["props"][:, 0].sum()), "npath": st["npath"], "nbatch": st["nbatch"],
+                         "nevals": st["nevals"], "nrestart": st["nrestart"]}
     if rank == 0 and not args.no_cp:
         cps = cp_search(args)
         if cps:

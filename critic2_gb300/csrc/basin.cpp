@@ -39,9 +39,11 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "c2g_internal.h"
+#include "forkjoin.h"
 #include "gpath.h"
 
 namespace c2g {
@@ -152,7 +154,8 @@ struct Ray {
   double riaprox = 0.0, raprox = kVBig, rother = kVBig;
   double xin[3], xfin[3], xi[3], xf[3], xmed[3];
   double rlim = -1.0;
-  int nwarn = 0;
+  int nwarn = 0;      // paths of this ray that ended with ier > 0
+  int npath = 0, nrestart = 0;
   bool tracing = false;
   std::vector<double> rbeta;  // the ray's beta radii once it has shrunk one (else the defaults)
   Path path;
@@ -194,47 +197,67 @@ class BasinSearch {
         y.k = kNTries - 1;
         next_inner(y);
       }
-    BatchGrd bg(h_, std::max(1, (int)rays_.size()));
-    std::vector<double> xs(3 * rays_.size());
-    std::vector<int> who(rays_.size());
+    const long nr = (long)rays_.size();
+    BatchGrd bg(h_, std::max(1, (int)nr));
+    std::vector<double> xs(3 * nr);
+    std::vector<int> who(nr);
+    std::vector<char> need(nr);
+    // host threads for the rays' step logic (the rays are independent)
+    const int hw = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+    ForkJoin pool((int)std::max(1L, std::min((long)hw, nr / 64)));
     for (;;) {
-      int m = 0;
-      for (size_t i = 0; i < rays_.size(); i++) {
-        Ray &y = rays_[i];
-        while (y.tracing) {
-          Path &p = y.path;
-          if (p.stage == 0) {
-            if (head(p, w_, ncp_, cpx_, cptyp_, y.rbeta.empty() ? rbeta_.data() : y.rbeta.data())) {
-              request_stage1(p);
-              break;
+      pool.run(nr, [&](long b, long e) {
+        for (long i = b; i < e; i++) {
+          Ray &y = rays_[i];
+          while (y.tracing) {
+            Path &p = y.path;
+            if (p.stage == 0) {
+              if (head(p, w_, ncp_, cpx_, cptyp_, y.rbeta.empty() ? rbeta_.data() : y.rbeta.data())) {
+                request_stage1(p);
+                break;
+              }
+              p.done = true;
             }
-            p.done = true;
+            if (p.done) {
+              y.tracing = false;
+              if (p.incstep) p.nstep++;
+              path_done(y);  // may start the ray's next path
+              continue;
+            }
+            break;
           }
-          if (p.done) {
-            y.tracing = false;
-            if (p.incstep) p.nstep++;
-            path_done(y);  // may start the ray's next path
-            continue;
-          }
-          break;
+          need[i] = y.tracing;
         }
-        if (!y.tracing) continue;
-        for (int j = 0; j < 3; j++) xs[3 * m + j] = y.path.req[j];
-        who[m++] = (int)i;
-      }
+      });
+      int m = 0;
+      for (long i = 0; i < nr; i++)
+        if (need[i]) who[m++] = (int)i;
       if (m == 0) break;
-      const double *rec = bg.eval(xs.data(), m);
-      for (int k = 0; k < m; k++) {
-        Path &p = rays_[who[k]].path;
-        const double *q = rec + (size_t)k * kRecNci;
-        if (p.stage == -1) take_start(p, q);
-        else advance(p, q);
-      }
+      pool.run(m, [&](long b, long e) {
+        for (long k = b; k < e; k++)
+          for (int j = 0; j < 3; j++) xs[3 * k + j] = rays_[who[k]].path.req[j];
+      });
+      const double *rec = bg.eval(xs.data(), m, &pool);
+      pool.run(m, [&](long b, long e) {
+        for (long k = b; k < e; k++) {
+          Path &p = rays_[who[k]].path;
+          const double *q = rec + (size_t)k * kRecNci;
+          if (p.stage == -1) take_start(p, q);
+          else advance(p, q);
+        }
+      });
     }
-    r.resize(rays_.size());
-    for (size_t i = 0; i < rays_.size(); i++) r[i] = rays_[i].rlim;
+    r.resize(nr);
+    for (long i = 0; i < nr; i++) {
+      const Ray &y = rays_[i];
+      r[i] = y.rlim;
+      npath_ += y.npath;
+      nwarn_ += y.nwarn;
+      nrestart_ += y.nrestart;
+    }
     nbatch_ = bg.launches();
     nevals_ = bg.evals();
+    threads_ = pool.threads();
   }
 
   long npath() const { return npath_; }
@@ -242,12 +265,13 @@ class BasinSearch {
   long nevals() const { return nevals_; }
   int nwarn() const { return nwarn_; }
   int nrestart() const { return nrestart_; }
+  int threads() const { return threads_; }
 
  private:
   void trace_from(Ray &y, const double x[3]) {
     start_path(y.path, x, 1);
     y.tracing = true;
-    npath_++;
+    y.npath++;
   }
   double end_dist(const Ray &y) const {
     const Attractor &a = att_[y.att];
@@ -328,7 +352,7 @@ class BasinSearch {
       if (y.rbeta.empty()) y.rbeta = rbeta_;
       if (std::sqrt(e2) <= y.rbeta[i]) {
         y.rbeta[i] *= 0.75;
-        nrestart_++;
+        y.nrestart++;
         restart_bisection(y);
         return;
       }
@@ -353,13 +377,12 @@ class BasinSearch {
 
   void path_done(Ray &y) {
     const Path &p = y.path;
-    if (p.ier > 0) nwarn_++;
+    if (p.ier > 0) y.nwarn++;
     if (y.phase == 0) {
       // :1314-1329
       if (p.ier == 3) {
         y.rother = std::min(y.rother, y.rin[y.k]);
       } else {
-        if (p.ier > 0) y.nwarn++;
         if (end_dist(y) <= kBsRNearNuc) {
           begin_outer(y);
           return;
@@ -374,7 +397,6 @@ class BasinSearch {
         if (y.raprox > y.riaprox) y.riaprox = y.raprox;
         y.raprox = y.rother;
       } else {
-        if (p.ier > 0) y.nwarn++;
         if (end_dist(y) > kBsRNearNuc) {
           begin_bisection(y);
           return;
@@ -392,7 +414,6 @@ class BasinSearch {
       } else if (p.ier == 3) {
         inside = false;
       } else {
-        y.nwarn++;
         inside = nearest_attractor(p.x) <= kBsRNearNuc;
       }
       for (int j = 0; j < 3; j++) (inside ? y.xi[j] : y.xf[j]) = y.xmed[j];
@@ -411,7 +432,7 @@ class BasinSearch {
   double prec_;
   std::vector<Ray> rays_;
   long npath_ = 0, nbatch_ = 0, nevals_ = 0;
-  int nwarn_ = 0, nrestart_ = 0;
+  int nwarn_ = 0, nrestart_ = 0, threads_ = 1;
 };
 
 // Valence density and its Laplacian at n host points (FP64, the EDF core

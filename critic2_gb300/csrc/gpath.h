@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "c2g_internal.h"
+#include "forkjoin.h"
 
 namespace c2g {
 namespace gpath {
@@ -74,7 +75,8 @@ class BatchGrd {
 
  public:
   // xyz(3, n) -> rec(10, n) with the nucleus rule applied to the gradient
-  const double *eval(const double *xyz, int n) {
+  // (over the pool's threads when one is given)
+  const double *eval(const double *xyz, int n, ForkJoin *pool = nullptr) {
     if (n <= 0) return h_rec_;
     if (n > cap_) fail(C2G_ERR_ARG, "gradient-path batch larger than its buffers");
     std::memcpy(h_in_, &n, sizeof(int));
@@ -86,22 +88,26 @@ class BatchGrd {
     evals_ += n;
     launches_++;
     const HostWfn &w = h_.host;
-    for (int i = 0; i < n; i++) {
-      double x[3];
-      for (int j = 0; j < 3; j++) {
-        double fr = (xyz[3 * i + j] - w.cell_lo[j]) / w.cell_aa[j];
-        if (fr < -1e-4 || fr > 1.0 + 1e-4) fr -= std::floor(fr);
-        x[j] = w.cell_lo[j] + fr * w.cell_aa[j];
-      }
-      for (int a = 0; a < w.natom; a++) {
-        const double dx = x[0] - w.xyz[3 * a], dy = x[1] - w.xyz[3 * a + 1], dz = x[2] - w.xyz[3 * a + 2];
-        if (std::sqrt(dx * dx + dy * dy + dz * dz) <= 1e-5) {
-          double *q = h_rec_ + (size_t)i * kRecNci;
-          q[1] = q[2] = q[3] = 0.0;
-          break;
+    const auto nucleus_rule = [&](long b, long e) {
+      for (long i = b; i < e; i++) {
+        double x[3];
+        for (int j = 0; j < 3; j++) {
+          double fr = (xyz[3 * i + j] - w.cell_lo[j]) / w.cell_aa[j];
+          if (fr < -1e-4 || fr > 1.0 + 1e-4) fr -= std::floor(fr);
+          x[j] = w.cell_lo[j] + fr * w.cell_aa[j];
+        }
+        for (int a = 0; a < w.natom; a++) {
+          const double dx = x[0] - w.xyz[3 * a], dy = x[1] - w.xyz[3 * a + 1], dz = x[2] - w.xyz[3 * a + 2];
+          if (std::sqrt(dx * dx + dy * dy + dz * dz) <= 1e-5) {
+            double *q = h_rec_ + (size_t)i * kRecNci;
+            q[1] = q[2] = q[3] = 0.0;
+            break;
+          }
         }
       }
-    }
+    };
+    if (pool) pool->run(n, nucleus_rule);
+    else nucleus_rule(0, n);
     return h_rec_;
   }
   long evals() const { return evals_; }
