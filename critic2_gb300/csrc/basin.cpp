@@ -8,15 +8,14 @@
 // point whose upward gradient path ends at the attractor and an outer point
 // whose path does not, and lim_surf (:1039-1126) bisects the bracket to
 // within the IAS precision, restarting with a smaller beta sphere when the
-// surface point falls inside one.  Each ray is a small state machine over
-// gradient paths; all rays' paths advance in lockstep (gpath.h), so one
-// Bogacki-Shampine stage of every live path is one batch of FP64
-// evaluations on the GPU.  The integrals follow integrals_lebedev /
-// integrals_gauleg (:1638-1877): a beta sphere of 0.95 times the smallest
-// surface radius integrated on a 170-point Lebedev rule
-// (sphereintegrals_lebedev, :829-854), plus each ray's radial Gauss-Legendre
-// quadrature (50 nodes) from the beta sphere to the surface
-// (int_radialquad, src/integration@proc.f90:384-486), summed as
+// surface point falls inside one.  Every ray runs on the device
+// (k_basin.cu): its state machine, its gradient paths (gpath.h) and the
+// FP64 evaluations they need, one block per ray, no host round trip.  The
+// integrals follow integrals_lebedev / integrals_gauleg (:1638-1877): a
+// beta sphere of 0.95 times the smallest surface radius integrated on a
+// 170-point Lebedev rule (sphereintegrals_lebedev, :829-854), plus each
+// ray's radial Gauss-Legendre quadrature (50 nodes) from the beta sphere to
+// the surface (int_radialquad, src/integration@proc.f90:384-486), summed as
 // lebedev_mquad (:591-642) or gauleg_mquad (:495-582).  The integrated
 // properties are critic2's molecular defaults (set_default_integprop,
 // src/systemmod@proc.f90:171-203): the valence density (Pop) and its
@@ -37,14 +36,14 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
 #include <limits>
 #include <numeric>
-#include <thread>
 #include <vector>
 
 #include "c2g_internal.h"
-#include "forkjoin.h"
 #include "gpath.h"
+#include "k_basin.h"
 
 namespace c2g {
 namespace {
@@ -81,8 +80,6 @@ struct DevBuf {
   }
 };
 
-constexpr double kBsRNearNuc = 3.1622776601683794e-3;  // bs_rnearnuc = sqrt(1e-5)
-constexpr int kNTries = 7;                             // bisect_msurface's bracket tries
 constexpr int kSphereLeb = 170;                        // bs_spherequad_nleb
 constexpr int kRadNodes = 50;                          // INT_radquad_nr (Gauss-Legendre)
 constexpr double kVBig = std::numeric_limits<double>::max();
@@ -145,22 +142,6 @@ void gauleg_nodes(int ntheta, int nphi, std::vector<Node> &nodes, std::vector<in
   }
 }
 
-// One (attractor, ray) of the surface search.
-struct Ray {
-  int att = 0, node = 0;
-  int phase = 0;  // 0 inner tries, 1 outer tries, 2 bisection, 3 done
-  int k = 0;      // position in the sorted tries
-  double rin[kNTries], rout[kNTries];  // tries, ascending
-  double riaprox = 0.0, raprox = kVBig, rother = kVBig;
-  double xin[3], xfin[3], xi[3], xf[3], xmed[3];
-  double rlim = -1.0;
-  int nwarn = 0;      // paths of this ray that ended with ier > 0
-  int npath = 0, nrestart = 0;
-  bool tracing = false;
-  std::vector<double> rbeta;  // the ray's beta radii once it has shrunk one (else the defaults)
-  Path path;
-};
-
 struct Attractor {
   int cp;           // index in the CP list
   double x[3];      // position
@@ -168,272 +149,98 @@ struct Attractor {
   double rmin, rminsame;
 };
 
-class BasinSearch {
- public:
-  BasinSearch(Handle &h, int ncp, const double *cpx, const int *cptyp, const std::vector<double> &rbeta,
-              const std::vector<Attractor> &att, const std::vector<Node> &nodes, double prec)
-      : h_(h), w_(h.host), ncp_(ncp), cpx_(cpx), cptyp_(cptyp), rbeta_(rbeta), att_(att), nodes_(nodes),
-        prec_(prec) {}
+int num_sms() {
+  int dev = 0, n = 0;
+  C2G_CUDA(cudaGetDevice(&dev));
+  C2G_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  return n;
+}
 
-  // Surface radii r[att * nray + ray]; counts of paths, warnings, restarts.
-  void run(std::vector<double> &r) {
-    const int nray = (int)nodes_.size(), natt = (int)att_.size();
-    rays_.resize((size_t)natt * nray);
-    const double amin = std::min({w_.cell_aa[0], w_.cell_aa[1], w_.cell_aa[2]});
-    const double amax = std::max({w_.cell_aa[0], w_.cell_aa[1], w_.cell_aa[2]});
-    for (int a = 0; a < natt; a++)
-      for (int j = 0; j < nray; j++) {
-        Ray &y = rays_[(size_t)a * nray + j];
-        y.att = a, y.node = j;
-        // bracket tries of bisect_msurface's first ray (:1290-1308,
-        // :1332-1350), each list sorted ascending (qcksort)
-        const double ti[kNTries] = {2e-5, 0.9 * att_[a].rmin, 0.99 * att_[a].rmin, 0.0, 0.0, 0.0, 0.0};
-        const double to[kNTries] = {amin, 0.99 * att_[a].rminsame, 0.75 * att_[a].rminsame, amax, amax, amax, amax};
-        std::copy(ti, ti + kNTries, y.rin);
-        std::copy(to, to + kNTries, y.rout);
-        std::sort(y.rin, y.rin + kNTries);
-        std::sort(y.rout, y.rout + kNTries);
-        y.phase = 0;
-        y.k = kNTries - 1;
-        next_inner(y);
-      }
-    const long nr = (long)rays_.size();
-    BatchGrd bg(h_, std::max(1, (int)nr));
-    std::vector<double> xs(3 * nr);
-    std::vector<int> who(nr);
-    std::vector<char> need(nr);
-    // host threads for the rays' step logic (the rays are independent)
-    const int hw = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
-    ForkJoin pool((int)std::max(1L, std::min((long)hw, nr / 64)));
-    for (;;) {
-      pool.run(nr, [&](long b, long e) {
-        for (long i = b; i < e; i++) {
-          Ray &y = rays_[i];
-          while (y.tracing) {
-            Path &p = y.path;
-            if (p.stage == 0) {
-              if (head(p, w_, ncp_, cpx_, cptyp_, y.rbeta.empty() ? rbeta_.data() : y.rbeta.data())) {
-                request_stage1(p);
-                break;
-              }
-              p.done = true;
-            }
-            if (p.done) {
-              y.tracing = false;
-              if (p.incstep) p.nstep++;
-              path_done(y);  // may start the ray's next path
-              continue;
-            }
-            break;
-          }
-          need[i] = y.tracing;
-        }
-      });
-      int m = 0;
-      for (long i = 0; i < nr; i++)
-        if (need[i]) who[m++] = (int)i;
-      if (m == 0) break;
-      pool.run(m, [&](long b, long e) {
-        for (long k = b; k < e; k++)
-          for (int j = 0; j < 3; j++) xs[3 * k + j] = rays_[who[k]].path.req[j];
-      });
-      const double *rec = bg.eval(xs.data(), m, &pool);
-      pool.run(m, [&](long b, long e) {
-        for (long k = b; k < e; k++) {
-          Path &p = rays_[who[k]].path;
-          const double *q = rec + (size_t)k * kRecNci;
-          if (p.stage == -1) take_start(p, q);
-          else advance(p, q);
-        }
-      });
-    }
-    r.resize(nr);
-    for (long i = 0; i < nr; i++) {
-      const Ray &y = rays_[i];
-      r[i] = y.rlim;
-      npath_ += y.npath;
-      nwarn_ += y.nwarn;
-      nrestart_ += y.nrestart;
-    }
-    nbatch_ = bg.launches();
-    nevals_ = bg.evals();
-    threads_ = pool.threads();
-  }
+template <class T>
+T *upload(std::deque<DevBuf> &keep, const std::vector<T> &v) {
+  keep.emplace_back(sizeof(T) * std::max<size_t>(v.size(), 1));
+  if (!v.empty()) C2G_CUDA(cudaMemcpy(keep.back().p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return keep.back().as<T>();
+}
 
-  long npath() const { return npath_; }
-  long nbatch() const { return nbatch_; }
-  long nevals() const { return nevals_; }
-  int nwarn() const { return nwarn_; }
-  int nrestart() const { return nrestart_; }
-  int threads() const { return threads_; }
+template <class T>
+std::vector<T> download(const T *d, size_t n) {
+  std::vector<T> v(n);
+  if (n) C2G_CUDA(cudaMemcpy(v.data(), d, sizeof(T) * n, cudaMemcpyDeviceToHost));
+  return v;
+}
 
- private:
-  void trace_from(Ray &y, const double x[3]) {
-    start_path(y.path, x, 1);
-    y.tracing = true;
-    y.npath++;
-  }
-  double end_dist(const Ray &y) const {
-    const Attractor &a = att_[y.att];
-    double d2 = 0.0;
-    for (int j = 0; j < 3; j++) d2 += (y.path.x[j] - a.x[j]) * (y.path.x[j] - a.x[j]);
-    return std::sqrt(d2);
-  }
-  void point_at(const Ray &y, double r, double x[3]) const {
-    const Attractor &a = att_[y.att];
-    const Node &n = nodes_[y.node];
-    for (int j = 0; j < 3; j++) x[j] = a.x[j] + r * n.u[j];
-  }
-
-  // inner tries, largest radius first (:1309-1330)
-  void next_inner(Ray &y) {
-    if (y.k < 0) {
-      begin_outer(y);
-      return;
-    }
-    y.riaprox = y.rin[y.k];
-    double x[3];
-    point_at(y, y.riaprox, x);
-    trace_from(y, x);
-  }
-  void begin_outer(Ray &y) {
-    y.phase = 1;
-    y.k = 0;
-    y.raprox = y.rother;
-    next_outer(y);
-  }
-  // outer tries, smallest radius first; a try must improve on a bisection
-  // step of the bracket found so far (:1352-1394)
-  void next_outer(Ray &y) {
-    while (y.k < kNTries) {
-      y.raprox = y.rout[y.k];
-      if (y.raprox > (y.rother + y.riaprox) / 2.0 || y.raprox < y.riaprox) {
-        y.raprox = y.rother;
-        y.k++;
-        continue;
-      }
-      double x[3];
-      point_at(y, y.raprox, x);
-      trace_from(y, x);
-      return;
-    }
-    begin_bisection(y);
-  }
-  void begin_bisection(Ray &y) {
-    if (y.raprox == kVBig || y.riaprox == 0.0)
-      fail(C2G_ERR_NUMERIC, "basin bisection: can not find ray limits (attractor " + std::to_string(att_[y.att].cp) +
-                                ", ray " + std::to_string(y.node) + ")");
-    point_at(y, y.riaprox, y.xin);
-    point_at(y, y.raprox, y.xfin);
-    y.phase = 2;
-    restart_bisection(y);
-  }
-  // lim_surf (:1039-1126) from its label 1
-  void restart_bisection(Ray &y) {
-    for (int j = 0; j < 3; j++) y.xi[j] = y.xin[j], y.xf[j] = y.xfin[j];
-    next_bisection(y);
-  }
-  void next_bisection(Ray &y) {
-    double d2 = 0.0;
-    for (int j = 0; j < 3; j++) d2 += (y.xi[j] - y.xf[j]) * (y.xi[j] - y.xf[j]);
-    if (std::sqrt(d2) > prec_) {
-      for (int j = 0; j < 3; j++) y.xmed[j] = 0.5 * (y.xi[j] + y.xf[j]);
-      trace_from(y, y.xmed);
-      return;
-    }
-    for (int j = 0; j < 3; j++) y.xmed[j] = 0.5 * (y.xi[j] + y.xf[j]);
-    // a surface point inside the beta sphere of a CP of the attractor's
-    // type shrinks that sphere and restarts the bisection (:1110-1124)
-    const int typ = att_[y.att].typ;
-    for (int i = 0; i < ncp_; i++) {
-      if (cptyp_[i] != typ) continue;
-      double e2 = 0.0;
-      for (int j = 0; j < 3; j++) e2 += (cpx_[3 * i + j] - y.xmed[j]) * (cpx_[3 * i + j] - y.xmed[j]);
-      if (y.rbeta.empty()) y.rbeta = rbeta_;
-      if (std::sqrt(e2) <= y.rbeta[i]) {
-        y.rbeta[i] *= 0.75;
-        y.nrestart++;
-        restart_bisection(y);
-        return;
-      }
-    }
-    double r2 = 0.0;
-    for (int j = 0; j < 3; j++) r2 += (y.xmed[j] - att_[y.att].x[j]) * (y.xmed[j] - att_[y.att].x[j]);
-    y.rlim = std::sqrt(r2);
-    y.phase = 3;
-  }
-
-  // nearest CP of the nuclear type (-3) to x: field%nearest_cp with type
-  double nearest_attractor(const double x[3]) const {
-    double best = kVBig;
-    for (int i = 0; i < ncp_; i++) {
-      if (cptyp_[i] != -3) continue;
-      double d2 = 0.0;
-      for (int j = 0; j < 3; j++) d2 += (cpx_[3 * i + j] - x[j]) * (cpx_[3 * i + j] - x[j]);
-      best = std::min(best, std::sqrt(d2));
-    }
-    return best;
-  }
-
-  void path_done(Ray &y) {
-    const Path &p = y.path;
-    if (p.ier > 0) y.nwarn++;
-    if (y.phase == 0) {
-      // :1314-1329
-      if (p.ier == 3) {
-        y.rother = std::min(y.rother, y.rin[y.k]);
-      } else {
-        if (end_dist(y) <= kBsRNearNuc) {
-          begin_outer(y);
-          return;
-        }
-        y.rother = std::min(y.rother, y.rin[y.k]);
-      }
-      y.k--;
-      next_inner(y);
-    } else if (y.phase == 1) {
-      // :1366-1393
-      if (p.ier == 3) {
-        if (y.raprox > y.riaprox) y.riaprox = y.raprox;
-        y.raprox = y.rother;
-      } else {
-        if (end_dist(y) > kBsRNearNuc) {
-          begin_bisection(y);
-          return;
-        }
-        if (y.raprox > y.riaprox) y.riaprox = y.raprox;
-        y.raprox = y.rother;
-      }
-      y.k++;
-      next_outer(y);
-    } else {
-      // :1078-1105
-      bool inside;
-      if (p.ier <= 0) {
-        inside = end_dist(y) <= kBsRNearNuc;
-      } else if (p.ier == 3) {
-        inside = false;
-      } else {
-        inside = nearest_attractor(p.x) <= kBsRNearNuc;
-      }
-      for (int j = 0; j < 3; j++) (inside ? y.xi[j] : y.xf[j]) = y.xmed[j];
-      next_bisection(y);
-    }
-  }
-
-  Handle &h_;
-  const HostWfn &w_;
-  int ncp_;
-  const double *cpx_;
-  const int *cptyp_;
-  const std::vector<double> &rbeta_;
-  const std::vector<Attractor> &att_;
-  const std::vector<Node> &nodes_;
-  double prec_;
-  std::vector<Ray> rays_;
-  long npath_ = 0, nbatch_ = 0, nevals_ = 0;
-  int nwarn_ = 0, nrestart_ = 0, threads_ = 1;
+struct SearchOut {
+  std::vector<double> r;
+  long npath = 0, nevals = 0;
+  int nwarn = 0, nrestart = 0;
 };
+
+// The surfaces of every (attractor, node) ray, traced on the device
+// (k_basin.cu): one block per ray at a time.
+SearchOut search_surfaces(Handle &h, int nc, const std::vector<double> &cpx, const std::vector<int> &typ,
+                          const std::vector<Attractor> &att, const std::vector<Node> &nodes, double prec) {
+  const HostWfn &w = h.host;
+  const int natt = (int)att.size(), nray = (int)nodes.size();
+  const long nr = (long)natt * nray;
+  std::deque<DevBuf> keep;  // device arrays of the search (not relocated)
+  std::vector<double> ax(3 * natt), rmin(natt), rms(natt), ru(3 * nray);
+  std::vector<int> at(natt);
+  for (int a = 0; a < natt; a++) {
+    for (int j = 0; j < 3; j++) ax[3 * a + j] = att[a].x[j];
+    rmin[a] = att[a].rmin, rms[a] = att[a].rminsame, at[a] = att[a].typ;
+  }
+  for (int i = 0; i < nray; i++)
+    for (int j = 0; j < 3; j++) ru[3 * i + j] = nodes[i].u[j];
+  PathGeom g = host_geom(w);
+  g.xyz = upload(keep, w.xyz);
+  g.z = upload(keep, w.z);
+  BasinDev b{};
+  b.ncp = nc;
+  b.cpx = upload(keep, cpx);
+  b.cptyp = upload(keep, typ);
+  b.prec = prec;
+  b.amin = std::min({w.cell_aa[0], w.cell_aa[1], w.cell_aa[2]});
+  b.amax = std::max({w.cell_aa[0], w.cell_aa[1], w.cell_aa[2]});
+  b.natt = natt;
+  b.nray = nray;
+  b.att_x = upload(keep, ax);
+  b.att_typ = upload(keep, at);
+  b.att_rmin = upload(keep, rmin);
+  b.att_rminsame = upload(keep, rms);
+  b.ray_u = upload(keep, ru);
+  const int grid = (int)std::max(1L, std::min(nr, (long)num_sms() * 3));
+  keep.emplace_back(sizeof(double) * (size_t)grid * std::max(nc, 1));
+  b.rbeta_scratch = keep.back().as<double>();
+  keep.emplace_back(sizeof(double) * std::max(nr, 1L));
+  b.rsurf = keep.back().as<double>();
+  int **ints[4] = {&b.ray_npath, &b.ray_nwarn, &b.ray_nrestart, &b.ray_err};
+  for (int **q : ints) {
+    keep.emplace_back(sizeof(int) * std::max(nr, 1L));
+    *q = keep.back().as<int>();
+  }
+  keep.emplace_back(sizeof(long) * std::max(nr, 1L));
+  b.ray_nevals = keep.back().as<long>();
+  SearchOut out;
+  if (nr > 0) {
+    launch_basin_rays(h.dev, g, b, grid, 0);
+    C2G_CUDA(cudaDeviceSynchronize());
+  }
+  out.r = download(b.rsurf, nr);
+  const std::vector<int> np = download(b.ray_npath, nr), nw = download(b.ray_nwarn, nr),
+                         rs = download(b.ray_nrestart, nr), er = download(b.ray_err, nr);
+  const std::vector<long> ne = download(b.ray_nevals, nr);
+  for (long i = 0; i < nr; i++) {
+    if (er[i]) {
+      static const char *why[4] = {"", "can not find ray limits", "too many beta-sphere restarts",
+                                   "evaluation limit reached"};
+      fail(C2G_ERR_NUMERIC, std::string("basin bisection: ") + why[er[i] & 3] + " (attractor " +
+                                std::to_string(att[i / nray].cp) + ", ray " + std::to_string(i % nray) + ")");
+    }
+    out.npath += np[i], out.nevals += ne[i], out.nwarn += nw[i], out.nrestart += rs[i];
+  }
+  return out;
+}
 
 // Valence density and its Laplacian at n host points (FP64, the EDF core
 // left out: grdall's fval and del2fval), in chunks.
@@ -567,9 +374,8 @@ int c2g_basin_integrals(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *c
       }
     }
     // the surfaces
-    std::vector<double> rbeta(nc, kRBeta), r;
-    BasinSearch bs(h, nc, cpx.data(), typ.data(), rbeta, att, nodes, iasprec);
-    bs.run(r);
+    const SearchOut so = search_surfaces(h, nc, cpx, typ, att, nodes, iasprec);
+    const std::vector<double> &r = so.r;
     // quadrature points: each attractor's beta sphere, then its rays and the
     // rays' surface points (the IAS error estimate)
     std::vector<Node> snodes;
@@ -664,11 +470,11 @@ int c2g_basin_integrals(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *c
     if (stats) {
       stats->natt = natt;
       stats->nray = nray;
-      stats->npath = bs.npath();
-      stats->nbatch = bs.nbatch();
-      stats->nevals = bs.nevals() + (long)xyz.size() / 3;
-      stats->nwarn = bs.nwarn();
-      stats->nrestart = bs.nrestart();
+      stats->npath = so.npath;
+      stats->nbatch = 1;
+      stats->nevals = so.nevals + (long)xyz.size() / 3;
+      stats->nwarn = so.nwarn;
+      stats->nrestart = so.nrestart;
       stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
   });

@@ -9,8 +9,10 @@
 // launch_fp64_index); the step logic (error control, beta spheres, bounce
 // detection) is O(1) per path and runs on the host between batches, in the
 // reference's order of operations, so the decisions are the ones a serial
-// trace makes with the same field values.  Used by the molecular graph
-// (graph.cpp) and the basin bisection (basin.cpp).
+// trace makes with the same field values.  The molecular graph
+// (graph.cpp) traces its paths this way; the path functions are also
+// compiled for the device, where the basin search (k_basin.cu) runs whole
+// rays without a host round trip.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -22,10 +24,33 @@
 #include <vector>
 
 #include "c2g_internal.h"
-#include "forkjoin.h"
+
+#if defined(__CUDACC__)
+#define C2G_HD __host__ __device__
+#else
+#define C2G_HD
+#endif
 
 namespace c2g {
 namespace gpath {
+
+// What a path needs of the molecule (host or device arrays): the nuclei,
+// their atomic numbers and the molecular cell.
+struct PathGeom {
+  int natom;
+  const double *xyz;  // 3 * natom
+  const int *z;
+  double cell_lo[3], cell_aa[3], molborder[3];
+};
+
+inline PathGeom host_geom(const HostWfn &w) {
+  PathGeom g;
+  g.natom = w.natom;
+  g.xyz = w.xyz.data();
+  g.z = w.z.data();
+  for (int j = 0; j < 3; j++) g.cell_lo[j] = w.cell_lo[j], g.cell_aa[j] = w.cell_aa[j], g.molborder[j] = w.molborder[j];
+  return g;
+}
 
 constexpr double kNavStep = 0.3, kNavMaxErr = 1e-4, kNavGradEps = 1e-7, kRBeta = 0.1;
 constexpr double kVSmall = 1e-80, kMinStep = 1e-12, kHFirst = 0.01;
@@ -75,8 +100,7 @@ class BatchGrd {
 
  public:
   // xyz(3, n) -> rec(10, n) with the nucleus rule applied to the gradient
-  // (over the pool's threads when one is given)
-  const double *eval(const double *xyz, int n, ForkJoin *pool = nullptr) {
+  const double *eval(const double *xyz, int n) {
     if (n <= 0) return h_rec_;
     if (n > cap_) fail(C2G_ERR_ARG, "gradient-path batch larger than its buffers");
     std::memcpy(h_in_, &n, sizeof(int));
@@ -106,8 +130,7 @@ class BatchGrd {
         }
       }
     };
-    if (pool) pool->run(n, nucleus_rule);
-    else nucleus_rule(0, n);
+    nucleus_rule(0, n);
     return h_rec_;
   }
   long evals() const { return evals_; }
@@ -135,8 +158,8 @@ struct Path {
   double req[3];  // point whose evaluation this path waits for
 };
 
-inline void unit(const double *q, double g[3]) {
-  const double m = std::sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+C2G_HD inline void unit(const double *q, double g[3]) {
+  const double m = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
   for (int j = 0; j < 3; j++) g[j] = q[1 + j] / (m + kVSmall);
 }
 
@@ -146,8 +169,8 @@ inline void unit(const double *q, double g[3]) {
 // null for the default sphere (min(Rbetadef, |hini| / 2) = 0.1 bohr), or
 // per-CP radii (up2beta; the CP list then starts with the nuclei in atom
 // order, so that a nucleus found first is CP idnuc).
-inline bool head(Path &p, const HostWfn &w, int ncp, const double *cpx, const int *cptyp,
-                 const double *rbeta = nullptr) {
+C2G_HD inline bool head(Path &p, const PathGeom &w, int ncp, const double *cpx, const int *cptyp,
+                        const double *rbeta = nullptr) {
   if (p.nstep > p.mstep) {
     p.nstep = p.mstep;
     p.ier = 2;
@@ -155,12 +178,12 @@ inline bool head(Path &p, const HostWfn &w, int ncp, const double *cpx, const in
   }
   double d2 = 0.0;
   for (int j = 0; j < 3; j++) d2 += (p.x[j] - p.xlast[j]) * (p.x[j] - p.xlast[j]);
-  p.plen += std::sqrt(d2);
+  p.plen += sqrt(d2);
   int idnuc = 0;
   double sphrad = 1e30;
   for (int a = 0; a < w.natom; a++) {
     const double dx = p.x[0] - w.xyz[3 * a], dy = p.x[1] - w.xyz[3 * a + 1], dz = p.x[2] - w.xyz[3 * a + 2];
-    const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
     if (d < sphrad) sphrad = d, idnuc = a;
   }
   bool have = false;
@@ -175,7 +198,7 @@ inline bool head(Path &p, const HostWfn &w, int ncp, const double *cpx, const in
   for (int i = 0; i < ncp; i++) {
     if (!((cptyp[i] == -3 && p.iup == 1) || (cptyp[i] == 3 && p.iup == -1))) continue;
     const double dx = p.x[0] - cpx[3 * i], dy = p.x[1] - cpx[3 * i + 1], dz = p.x[2] - cpx[3 * i + 2];
-    const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
     if (d < cprad) {
       have = true;
       idcp = i;
@@ -187,7 +210,7 @@ inline bool head(Path &p, const HostWfn &w, int ncp, const double *cpx, const in
     p.incstep = true;
     double e2 = 0.0;
     for (int j = 0; j < 3; j++) e2 += (p.x[j] - xcp[j]) * (p.x[j] - xcp[j]);
-    p.plen += std::sqrt(e2);
+    p.plen += sqrt(e2);
     for (int j = 0; j < 3; j++) p.x[j] = xcp[j];
     p.ier = 0;
     return false;
@@ -211,13 +234,13 @@ inline bool head(Path &p, const HostWfn &w, int ncp, const double *cpx, const in
   return true;
 }
 
-inline void request_stage1(Path &p) {
+C2G_HD inline void request_stage1(Path &p) {
   for (int j = 0; j < 3; j++) p.req[j] = p.x[j] + p.h0 * (0.5 * p.grdt[j]);
   p.stage = 1;
 }
 
 // After adaptive_stepper (:2672-2690): bounce history and step floor.
-inline void after_step(Path &p, bool ok) {
+C2G_HD inline void after_step(Path &p, bool ok) {
   p.nhist = p.nhist % kMHist + 1;
   double sc = 0.0;
   for (int j = 0; j < 3; j++) sc += (p.xlast[j] - p.xlast2[j]) * (p.x[j] - p.xlast[j]);
@@ -225,7 +248,7 @@ inline void after_step(Path &p, bool ok) {
   bool allneg = true;
   for (int k = 0; k < kMHist; k++) allneg = allneg && p.scal[k] < 0.0;
   ok = ok && !allneg;
-  if (!ok || std::fabs(p.h0) < kMinStep) {
+  if (!ok || fabs(p.h0) < kMinStep) {
     for (int j = 0; j < 3; j++) p.x[j] = p.xlast[j];
     p.ier = 1;
     p.done = true;
@@ -236,7 +259,7 @@ inline void after_step(Path &p, bool ok) {
 }
 
 // One evaluated BS stage of a path.
-inline void advance(Path &p, const double *q) {
+C2G_HD inline void advance(Path &p, const double *q) {
   if (p.stage == 1) {
     unit(q, p.ak2);
     for (int j = 0; j < 3; j++) p.req[j] = p.x[j] + p.h0 * (0.75 * p.ak2[j]);
@@ -254,16 +277,16 @@ inline void advance(Path &p, const double *q) {
       xerr[j] = p.x[j] + p.h0 * (7.0 / 24.0 * p.grdt[j] + 1.0 / 4.0 * p.ak2[j] + 1.0 / 3.0 * p.ak3[j] +
                                  1.0 / 8.0 * ak4[j]) - p.xout[j];
     for (int j = 0; j < 3; j++) p.gf[j] = q[1 + j], p.grdt[j] = ak4[j];
-    p.gfmod = std::sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-    const double nerr = std::sqrt(xerr[0] * xerr[0] + xerr[1] * xerr[1] + xerr[2] * xerr[2]);
+    p.gfmod = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    const double nerr = sqrt(xerr[0] * xerr[0] + xerr[1] * xerr[1] + xerr[2] * xerr[2]);
     if (nerr < kNavMaxErr) {
       for (int j = 0; j < 3; j++) p.x[j] = p.xout[j];
       if (p.first && nerr < kNavMaxErr / 10.0)
-        p.h0 = std::copysign(std::min(std::fabs(p.hini), std::fabs(1.6 * p.h0)), p.hini);
+        p.h0 = copysign(fmin(fabs(p.hini), fabs(1.6 * p.h0)), p.hini);
       after_step(p, true);
     } else {
       p.h0 = 0.9 * p.h0 * kNavMaxErr / nerr;
-      if (std::fabs(p.h0) < kVSmall) {
+      if (fabs(p.h0) < kVSmall) {
         after_step(p, false);
       } else {
         // the rejected trial's end-point gradient starts the next trial
@@ -277,7 +300,7 @@ inline void advance(Path &p, const double *q) {
 // Traces the paths to their ends (x, ier, nstep, plen in each Path).
 inline void trace_paths(Handle &h, std::vector<Path> &paths, int ncp, const double *cpx, const int *cptyp,
                         BatchGrd &bg) {
-  const HostWfn &w = h.host;
+  const PathGeom w = host_geom(h.host);
   const int n = (int)paths.size();
   std::vector<double> xs(3 * (size_t)n);
   std::vector<int> who(n);
@@ -316,26 +339,26 @@ inline void trace_paths(Handle &h, std::vector<Path> &paths, int ncp, const doub
 // A path from x going up (iup = 1) or down (iup = -1), field%gradient's
 // initial state; plen starts at |x - pathini| (pathini null: 0).  Its first
 // request is the field at x (stage -1).
-inline void start_path(Path &p, const double x[3], int iup, const double *pathini = nullptr) {
+C2G_HD inline void start_path(Path &p, const double x[3], int iup, const double *pathini = nullptr) {
   p = Path();
   p.iup = iup;
   p.hini = kNavStep * iup;
   p.h0 = kHFirst * iup;
-  p.mstep = (int)std::lround(10000 * 0.1 / std::fabs(p.hini));
+  p.mstep = (int)lround(10000 * 0.1 / fabs(p.hini));
   for (int k = 0; k < kMHist; k++) p.scal[k] = 1.0;
   double d2 = 0.0;
   for (int k = 0; k < 3; k++) {
     p.x[k] = p.xlast[k] = p.xlast2[k] = p.req[k] = x[k];
     if (pathini) d2 += (x[k] - pathini[k]) * (x[k] - pathini[k]);
   }
-  p.plen = std::sqrt(d2);
+  p.plen = sqrt(d2);
   p.stage = -1;
 }
 
 // The field at a path's start point (the answer to its stage -1 request).
-inline void take_start(Path &p, const double *q) {
+C2G_HD inline void take_start(Path &p, const double *q) {
   for (int j = 0; j < 3; j++) p.gf[j] = q[1 + j];
-  p.gfmod = std::sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  p.gfmod = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
   p.stage = 0;
 }
 

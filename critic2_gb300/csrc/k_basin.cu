@@ -1,0 +1,431 @@
+// The zero-flux surface search of critic2's INTEGRALS on the GPU, every ray
+// resident on the device: bisect_msurface (src/bisect@proc.f90:1208-1446)
+// and lim_surf (:1039-1126) for one (attractor, angular node) per block at
+// a time, over field%gradient's paths (gpath.h).
+//
+// Thread 0 of a block runs the ray's state machine (bracket tries, the
+// bisection, beta-sphere restarts, and the path's Bogacki-Shampine steps);
+// whenever the machine needs the field at a point, the whole block evaluates
+// it: the FP64 per-point evaluator's arithmetic (k_eval_fp64_pt: primitives
+// within critic2's cutoffs compacted in primitive order by ballots, one MO
+// per thread, a fixed-order block reduction), restricted to the density and
+// its gradient, at the point wrapped into the molecular cell, with the EDF
+// core and the nucleus rule (|grad| := 0 within 1e-5 bohr of a nucleus).
+// The values are the ones the batched host-driven tracer gets from the
+// per-point kernel, so the decisions are the same; no host round trip is
+// left between the steps.  Every loop is bounded: a path by its step
+// limit, a ray by its evaluation limit (kMaxRayEvals) and its restarts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <vector>
+
+#include "c2g_internal.h"
+#include "gpath.h"
+#include "gto.cuh"
+#include "k_basin.h"
+#include "points.cuh"
+
+namespace c2g {
+namespace {
+
+using namespace gpath;
+
+constexpr double kBsRNearNuc = 3.1622776601683794e-3;  // bs_rnearnuc = sqrt(1e-5)
+constexpr int kNTries = 7;
+constexpr int kMaxRestart = 16;           // beta-sphere restarts per ray
+constexpr long kMaxRayEvals = 1L << 22;   // field evaluations per ray
+
+// One ray's state (thread 0 of its block).
+struct RayState {
+  double xa[3], u[3];
+  int typ;
+  int phase, k;  // 0 inner tries, 1 outer tries, 2 bisection, 3 done
+  double rin[kNTries], rout[kNTries];
+  double riaprox, raprox, rother;
+  double xin[3], xfin[3], xi[3], xf[3], xmed[3];
+  double rlim;
+  int npath, nwarn, nrestart, err;
+  long nevals;
+  bool tracing, own_rb;
+  Path path;
+};
+
+struct Search {
+  PathGeom g;
+  BasinDev b;
+  double *rb;  // this block's beta radii (valid once own_rb)
+};
+
+__device__ void sort7(double (&v)[kNTries]) {
+  for (int i = 1; i < kNTries; i++) {
+    const double t = v[i];
+    int j = i - 1;
+    while (j >= 0 && v[j] > t) v[j + 1] = v[j], j--;
+    v[j + 1] = t;
+  }
+}
+
+__device__ double dist3(const double *a, const double *b) {
+  const double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+  return sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+}
+
+__device__ void trace_from(RayState &y, const double x[3]) {
+  start_path(y.path, x, 1);
+  y.tracing = true;
+  y.npath++;
+}
+
+__device__ void point_at(const RayState &y, double r, double x[3]) {
+  for (int j = 0; j < 3; j++) x[j] = y.xa[j] + r * y.u[j];
+}
+
+__device__ void begin_bisection(RayState &y, const Search &s);
+
+__device__ void begin_outer(RayState &y, const Search &s);
+
+// inner tries, largest radius first (:1309-1330)
+__device__ void next_inner(RayState &y, const Search &s) {
+  if (y.k < 0) {
+    begin_outer(y, s);
+    return;
+  }
+  y.riaprox = y.rin[y.k];
+  double x[3];
+  point_at(y, y.riaprox, x);
+  trace_from(y, x);
+}
+
+// outer tries, smallest first, each better than a bisection step (:1352-1394)
+__device__ void next_outer(RayState &y, const Search &s) {
+  while (y.k < kNTries) {
+    y.raprox = y.rout[y.k];
+    if (y.raprox > (y.rother + y.riaprox) / 2.0 || y.raprox < y.riaprox) {
+      y.raprox = y.rother;
+      y.k++;
+      continue;
+    }
+    double x[3];
+    point_at(y, y.raprox, x);
+    trace_from(y, x);
+    return;
+  }
+  begin_bisection(y, s);
+}
+
+__device__ void begin_outer(RayState &y, const Search &s) {
+  y.phase = 1;
+  y.k = 0;
+  y.raprox = y.rother;
+  next_outer(y, s);
+}
+
+__device__ void next_bisection(RayState &y, const Search &s);
+
+__device__ void begin_bisection(RayState &y, const Search &s) {
+  if (y.raprox == DBL_MAX || y.riaprox == 0.0) {
+    y.err = 1;  // "Can not find ray limits"
+    y.phase = 3;
+    return;
+  }
+  point_at(y, y.riaprox, y.xin);
+  point_at(y, y.raprox, y.xfin);
+  y.phase = 2;
+  // lim_surf from its label 1
+  for (int j = 0; j < 3; j++) y.xi[j] = y.xin[j], y.xf[j] = y.xfin[j];
+  next_bisection(y, s);
+}
+
+__device__ void next_bisection(RayState &y, const Search &s) {
+  for (;;) {
+    for (int j = 0; j < 3; j++) y.xmed[j] = 0.5 * (y.xi[j] + y.xf[j]);
+    if (dist3(y.xi, y.xf) > s.b.prec) {
+      trace_from(y, y.xmed);
+      return;
+    }
+    // a surface point in the beta sphere of a CP of the attractor's type
+    // shrinks that sphere (the ray's own copy) and restarts from the
+    // bracket (:1110-1124)
+    bool again = false;
+    for (int i = 0; i < s.b.ncp && !again; i++) {
+      if (s.b.cptyp[i] != y.typ) continue;
+      const double rbi = y.own_rb ? s.rb[i] : kRBeta;
+      if (dist3(s.b.cpx + 3 * i, y.xmed) > rbi) continue;
+      if (y.nrestart >= kMaxRestart) {
+        y.err = 2;
+        y.phase = 3;
+        return;
+      }
+      if (!y.own_rb) {
+        for (int c = 0; c < s.b.ncp; c++) s.rb[c] = kRBeta;
+        y.own_rb = true;
+      }
+      s.rb[i] *= 0.75;
+      y.nrestart++;
+      again = true;
+    }
+    if (!again) break;
+    for (int j = 0; j < 3; j++) y.xi[j] = y.xin[j], y.xf[j] = y.xfin[j];
+  }
+  y.rlim = dist3(y.xmed, y.xa);
+  y.phase = 3;
+}
+
+__device__ double nearest_attractor(const Search &s, const double *x) {
+  double best = DBL_MAX;
+  for (int i = 0; i < s.b.ncp; i++)
+    if (s.b.cptyp[i] == -3) best = fmin(best, dist3(s.b.cpx + 3 * i, x));
+  return best;
+}
+
+__device__ void path_done(RayState &y, const Search &s) {
+  const Path &p = y.path;
+  if (p.ier > 0) y.nwarn++;
+  const double d = dist3(p.x, y.xa);
+  if (y.phase == 0) {
+    if (p.ier != 3 && d <= kBsRNearNuc) {
+      begin_outer(y, s);
+      return;
+    }
+    y.rother = fmin(y.rother, y.rin[y.k]);
+    y.k--;
+    next_inner(y, s);
+  } else if (y.phase == 1) {
+    if (p.ier != 3 && d > kBsRNearNuc) {
+      begin_bisection(y, s);
+      return;
+    }
+    if (y.raprox > y.riaprox) y.riaprox = y.raprox;
+    y.raprox = y.rother;
+    y.k++;
+    next_outer(y, s);
+  } else {
+    bool inside;
+    if (p.ier <= 0) inside = d <= kBsRNearNuc;
+    else if (p.ier == 3) inside = false;
+    else inside = nearest_attractor(s, p.x) <= kBsRNearNuc;
+    for (int j = 0; j < 3; j++) (inside ? y.xi[j] : y.xf[j]) = y.xmed[j];
+    next_bisection(y, s);
+  }
+}
+
+__device__ void ray_init(RayState &y, const Search &s, int att, int node) {
+  const BasinDev &b = s.b;
+  for (int j = 0; j < 3; j++) y.xa[j] = b.att_x[3 * att + j], y.u[j] = b.ray_u[3 * node + j];
+  y.typ = b.att_typ[att];
+  const double rmin = b.att_rmin[att], rms = b.att_rminsame[att];
+  const double ti[kNTries] = {2e-5, 0.9 * rmin, 0.99 * rmin, 0.0, 0.0, 0.0, 0.0};
+  const double to[kNTries] = {b.amin, 0.99 * rms, 0.75 * rms, b.amax, b.amax, b.amax, b.amax};
+  for (int i = 0; i < kNTries; i++) y.rin[i] = ti[i], y.rout[i] = to[i];
+  sort7(y.rin);
+  sort7(y.rout);
+  y.riaprox = 0.0, y.raprox = DBL_MAX, y.rother = DBL_MAX;
+  y.rlim = -1.0;
+  y.npath = y.nwarn = y.nrestart = y.err = 0;
+  y.nevals = 0;
+  y.tracing = false, y.own_rb = false;
+  y.phase = 0;
+  y.k = kNTries - 1;
+  next_inner(y, s);
+}
+
+// Advances the ray until it needs the field at a point (true, x) or is done.
+__device__ bool ray_request(RayState &y, const Search &s, double x[3]) {
+  while (y.tracing) {
+    Path &p = y.path;
+    if (p.stage == 0) {
+      if (head(p, s.g, s.b.ncp, s.b.cpx, s.b.cptyp, y.own_rb ? s.rb : nullptr)) {
+        request_stage1(p);
+        break;
+      }
+      p.done = true;
+    }
+    if (p.done) {
+      y.tracing = false;
+      if (p.incstep) p.nstep++;
+      path_done(y, s);
+      continue;
+    }
+    break;
+  }
+  if (!y.tracing) return false;
+  if (y.nevals >= kMaxRayEvals) {
+    y.err = 3;
+    y.tracing = false;
+    y.phase = 3;
+    return false;
+  }
+  for (int j = 0; j < 3; j++) x[j] = y.path.req[j];
+  return true;
+}
+
+// The block's evaluation of rho and its gradient at x (wrapped into the
+// cell), into q[0..3] of thread 0.
+template <int MPT>
+__device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_chi, int *s_k, int *s_wn,
+                           double *s_red, double (&q)[4]) {
+  const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+  double x[3] = {xin[0], xin[1], xin[2]};
+  wrap_cell(w, x);
+  double acc[MPT][4];
+#pragma unroll
+  for (int m = 0; m < MPT; m++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[m][c] = 0.0;
+  for (int k0 = 0; k0 < w.npri; k0 += 256) {
+    const int ip = k0 + tid;
+    double chi[4];
+    bool in = false;
+    if (ip < w.npri) {
+      const PrimF64 pr = w.prim[ip];
+      const double4 A = w.atoms[pr.atom];
+      const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+      const double dd = dx * dx + dy * dy + dz * dz;
+      if (dd <= A.w) {
+        const double dist = sqrt(dd);
+        if (!(dist > pr.dran)) {
+          in = true;
+          chi_eval<4>(dx, dy, dz, pr.e, pr.lpack, exp(-pr.e * (dist * dist)), chi);
+        }
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) s_wn[wp] = __popc(bal);
+    __syncthreads();
+    int base = 0, nact = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      base += i < wp ? s_wn[i] : 0;
+      nact += s_wn[i];
+    }
+    if (in) {
+      const int slot = base + __popc(bal & ((1u << lane) - 1u));
+#pragma unroll
+      for (int c = 0; c < 4; c++) s_chi[slot * 4 + c] = chi[c];
+      s_k[slot] = ip;
+    }
+    __syncthreads();
+    // threads without an MO skip the contraction (their sums stay zero)
+#pragma unroll 2
+    for (int j = 0; j < (tid < w.nmo ? nact : 0); j++) {
+      const double *crow = w.cmo + (size_t)s_k[j] * w.nmo_pad;
+      double ch[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) ch[c] = s_chi[j * 4 + c];
+#pragma unroll
+      for (int m = 0; m < MPT; m++) {
+        const int mo = tid + 256 * m;
+        const double cm = mo < w.nmo ? __ldg(crow + mo) : 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[m][c] = fma(cm, ch[c], acc[m][c]);
+      }
+    }
+    __syncthreads();
+  }
+  double r[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int m = 0; m < MPT; m++) {
+    const int mo = tid + 256 * m;
+    const double o = mo < w.nmo ? w.occ[mo] : 0.0;
+    const double p0 = acc[m][0];
+    r[0] += o * p0 * p0;
+    r[1] += 2.0 * o * p0 * acc[m][1];
+    r[2] += 2.0 * o * p0 * acc[m][2];
+    r[3] += 2.0 * o * p0 * acc[m][3];
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    for (int off = 16; off; off >>= 1) r[c] += __shfl_xor_sync(0xffffffffu, r[c], off);
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < 4; c++) s_red[wp * 4 + c] = r[c];
+  __syncthreads();
+  if (wp == 0) {
+    double core_c = 0.0;
+    if (w.nedf) {
+      double core[10];
+      edf_core_warp(w, x, core);
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (c == lane) core_c = core[c];
+    }
+    if (lane < 4) {
+      double sum = 0.0;
+      for (int i = 0; i < 8; i++) sum += s_red[i * 4 + lane];
+      s_red[32 + lane] = sum + core_c;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int c = 0; c < 4; c++) q[c] = s_red[32 + c];
+    // the nucleus rule, at the wrapped point
+    for (int a = 0; a < w.natom; a++) {
+      const double4 A = w.atoms[a];
+      const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+      if (sqrt(dx * dx + dy * dy + dz * dz) <= 1e-5) {
+        q[1] = q[2] = q[3] = 0.0;
+        break;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int MPT>
+__global__ void __launch_bounds__(256) k_basin_rays(DevWfn w, PathGeom g, BasinDev b) {
+  __shared__ double s_chi[256 * 4];
+  __shared__ int s_k[256];
+  __shared__ int s_wn[8];
+  __shared__ double s_red[8 * 4 + 4];
+  __shared__ double s_x[3];
+  __shared__ int s_more;
+  // the ray's state, used by thread 0 only (set by ray_init)
+  __shared__ __align__(16) unsigned char s_ray[sizeof(RayState)];
+  RayState &y = *reinterpret_cast<RayState *>(s_ray);
+  const Search s{g, b, b.rbeta_scratch + (size_t)blockIdx.x * (b.ncp > 0 ? b.ncp : 1)};
+  const long nr = (long)b.natt * b.nray;
+  for (long ray = blockIdx.x; ray < nr; ray += gridDim.x) {
+    if (threadIdx.x == 0) ray_init(y, s, (int)(ray / b.nray), (int)(ray % b.nray));
+    for (;;) {
+      if (threadIdx.x == 0) {
+        double x[3];
+        s_more = ray_request(y, s, x) ? 1 : 0;
+        if (s_more) s_x[0] = x[0], s_x[1] = x[1], s_x[2] = x[2];
+      }
+      __syncthreads();
+      if (!s_more) break;
+      const double xx[3] = {s_x[0], s_x[1], s_x[2]};
+      double q[4];
+      eval_block<MPT>(w, xx, s_chi, s_k, s_wn, s_red, q);
+      if (threadIdx.x == 0) {
+        y.nevals++;
+        double rec[4] = {q[0], q[1], q[2], q[3]};
+        if (y.path.stage == -1) take_start(y.path, rec);
+        else advance(y.path, rec);
+      }
+    }
+    if (threadIdx.x == 0) {
+      b.rsurf[ray] = y.rlim;
+      b.ray_npath[ray] = y.npath;
+      b.ray_nwarn[ray] = y.nwarn;
+      b.ray_nrestart[ray] = y.nrestart;
+      b.ray_err[ray] = y.err;
+      b.ray_nevals[ray] = y.nevals;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+void launch_basin_rays(const DevWfn &w, const PathGeom &g, const BasinDev &b, int grid, cudaStream_t st) {
+  if (w.nmo <= 256) k_basin_rays<1><<<grid, 256, 0, st>>>(w, g, b);
+  else if (w.nmo <= 512) k_basin_rays<2><<<grid, 256, 0, st>>>(w, g, b);
+  else k_basin_rays<4><<<grid, 256, 0, st>>>(w, g, b);
+  C2G_CUDA(cudaGetLastError());
+}
+
+}  // namespace c2g

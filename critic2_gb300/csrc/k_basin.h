@@ -1,0 +1,32 @@
+// Device side of the basin-integral surface search (k_basin.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "c2g_internal.h"
+#include "gpath.h"
+
+namespace c2g {
+
+// One search: the CP list, the attractors and the rays (all device arrays),
+// and the per-ray outputs.  Ray r = attractor r / nray, node r % nray.
+struct BasinDev {
+  int ncp;
+  const double *cpx;  // 3 * ncp
+  const int *cptyp;
+  double prec, amin, amax;  // IAS precision; smallest and largest cell lengths
+  int natt, nray;
+  const double *att_x;  // 3 * natt
+  const int *att_typ;
+  const double *att_rmin, *att_rminsame;
+  const double *ray_u;      // 3 * nray unit directions
+  double *rbeta_scratch;    // grid * ncp: the beta radii of a block's current ray
+  double *rsurf;            // natt * nray
+  int *ray_npath, *ray_nwarn, *ray_nrestart, *ray_err;  // err: 1 no bracket, 2 restarts, 3 evaluations
+  long *ray_nevals;
+};
+
+// Every ray of the search, one block of 256 threads per ray at a time.
+void launch_basin_rays(const DevWfn &w, const gpath::PathGeom &g, const BasinDev &b, int grid, cudaStream_t st);
+
+}  // namespace c2g

@@ -341,8 +341,9 @@ __global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, Src src, Sink si
         s_k[slot] = ip;
       }
       __syncthreads();
+      // threads without an MO skip the contraction (their sums stay zero)
 #pragma unroll 2
-      for (int j = 0; j < nact; j++) {
+      for (int j = 0; j < (tid < w.nmo ? nact : 0); j++) {
         const double *crow = w.cmo + (size_t)s_k[j] * w.nmo_pad;
         double ch[10];
 #pragma unroll
