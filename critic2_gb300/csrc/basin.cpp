@@ -9,7 +9,7 @@
 // whose path does not, and lim_surf (:1039-1126) bisects the bracket to
 // within the IAS precision, restarting with a smaller beta sphere when the
 // surface point falls inside one.  Every ray runs on the device
-// (k_basin.cu): its state machine, its gradient paths (gpath.h) and the
+// (k_gpath.cu): its state machine, its gradient paths (gpath.h) and the
 // FP64 evaluations they need, one block per ray, no host round trip.  The
 // integrals follow integrals_lebedev / integrals_gauleg (:1638-1877): a
 // beta sphere of 0.95 times the smallest surface radius integrated on a
@@ -43,7 +43,7 @@
 
 #include "c2g_internal.h"
 #include "gpath.h"
-#include "k_basin.h"
+#include "k_gpath.h"
 
 namespace c2g {
 namespace {
@@ -177,7 +177,7 @@ struct SearchOut {
 };
 
 // The surfaces of every (attractor, node) ray, traced on the device
-// (k_basin.cu): one block per ray at a time.
+// (k_gpath.cu): one block per ray at a time.
 SearchOut search_surfaces(Handle &h, int nc, const std::vector<double> &cpx, const std::vector<int> &typ,
                           const std::vector<Attractor> &att, const std::vector<Node> &nodes, double prec) {
   const HostWfn &w = h.host;

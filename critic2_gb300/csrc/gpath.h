@@ -1,18 +1,17 @@
-// Gradient paths of a molecular wavefunction field, traced in lockstep on
-// the GPU: field%gradient (src/fieldmod@proc.f90:2500-2732) with critic2's
-// default navigation: the Bogacki-Shampine 2(3) stepper (:2860-2890) inside
-// adaptive_stepper (:2737-2830), step 0.3, maxerr 1e-4, gradeps 1e-7, beta
-// spheres 0.1 (src/global@proc.F90:858-861, src/global.f90:41).
+// Gradient paths of a molecular wavefunction field: field%gradient
+// (src/fieldmod@proc.f90:2500-2732) with critic2's default navigation: the
+// Bogacki-Shampine 2(3) stepper (:2860-2890) inside adaptive_stepper
+// (:2737-2830), step 0.3, maxerr 1e-4, gradeps 1e-7, beta spheres 0.1
+// (src/global@proc.F90:858-861, src/global.f90:41).
 //
-// Every Runge-Kutta stage of every live path is one batch of field
-// evaluations, done by the FP64 per-point kernel (k_eval_fp64_pt through
-// launch_fp64_index); the step logic (error control, beta spheres, bounce
-// detection) is O(1) per path and runs on the host between batches, in the
-// reference's order of operations, so the decisions are the ones a serial
-// trace makes with the same field values.  The molecular graph
-// (graph.cpp) traces its paths this way; the path functions are also
-// compiled for the device, where the basin search (k_basin.cu) runs whole
-// rays without a host round trip.
+// A path is a small state machine: head() does the part of a step before
+// the Runge-Kutta stages (path length, beta spheres, molecular cell, new
+// CP), each stage asks for the field at one point (req) and advance() takes
+// it, in the reference's order of operations, so the decisions are the ones
+// a serial trace makes with the same field values.  The functions compile
+// for host and device: the device kernels (k_gpath.cu) run whole paths
+// without a host round trip.  BatchGrd evaluates the field at a batch of
+// host points (the FP64 per-point kernel, then the nucleus rule).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -295,45 +294,6 @@ C2G_HD inline void advance(Path &p, const double *q) {
       }
     }
   }
-}
-
-// Traces the paths to their ends (x, ier, nstep, plen in each Path).
-inline void trace_paths(Handle &h, std::vector<Path> &paths, int ncp, const double *cpx, const int *cptyp,
-                        BatchGrd &bg) {
-  const PathGeom w = host_geom(h.host);
-  const int n = (int)paths.size();
-  std::vector<double> xs(3 * (size_t)n);
-  std::vector<int> who(n);
-  // field at the start points
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < 3; j++) xs[3 * i + j] = paths[i].x[j];
-  const double *rec = bg.eval(xs.data(), n);
-  for (int i = 0; i < n; i++) {
-    const double *q = rec + (size_t)i * kRecNci;
-    for (int j = 0; j < 3; j++) paths[i].gf[j] = q[1 + j];
-    paths[i].gfmod = std::sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-  }
-  for (;;) {
-    int m = 0;
-    for (int i = 0; i < n; i++) {
-      Path &p = paths[i];
-      if (p.done) continue;
-      if (p.stage == 0) {
-        if (!head(p, w, ncp, cpx, cptyp)) {
-          p.done = true;
-          continue;
-        }
-        request_stage1(p);
-      }
-      for (int j = 0; j < 3; j++) xs[3 * m + j] = p.req[j];
-      who[m++] = i;
-    }
-    if (m == 0) break;
-    rec = bg.eval(xs.data(), m);
-    for (int k = 0; k < m; k++) advance(paths[who[k]], rec + (size_t)k * kRecNci);
-  }
-  for (Path &p : paths)
-    if (p.incstep) p.nstep++;
 }
 
 // A path from x going up (iup = 1) or down (iup = -1), field%gradient's

@@ -6,12 +6,11 @@
 // (:2737-2830), step 0.3, maxerr 1e-4, gradeps 1e-7, beta spheres 0.1
 // (src/global@proc.F90:858-861, src/global.f90:41).
 //
-// The paths advance in lockstep: every Runge-Kutta stage of every live path
-// is one batch of field evaluations, done on the GPU by the FP64 per-point
-// kernel (k_eval_fp64_pt through launch_fp64_index); the step logic (error
-// control, beta spheres, bounce detection) is O(1) per path and runs on the
-// host between batches, in the reference's order of operations, so the
-// decisions are the ones a serial trace makes with the same field values.
+// The paths run on the GPU (k_gpath.cu), one block per path: thread 0
+// takes field%gradient's steps (error control, beta spheres, bounce
+// detection, in the reference's order of operations) and the block
+// evaluates the FP64 field each step needs, with the per-point kernel's
+// arithmetic, so no step waits for the host.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,11 +22,74 @@
 
 #include "c2g_internal.h"
 #include "gpath.h"
+#include "k_gpath.h"
 
 namespace c2g {
 namespace {
 
 using namespace gpath;
+
+// Device copy of a host array, freed with the object.
+template <class T>
+struct DevArr {
+  T *p = nullptr;
+  explicit DevArr(const std::vector<T> &v) : DevArr(v.size()) {
+    if (!v.empty()) C2G_CUDA(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  }
+  explicit DevArr(size_t n) {
+    const cudaError_t e = cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1));
+    if (e != cudaSuccess) fail(C2G_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  ~DevArr() {
+    if (p) cudaFree(p);
+  }
+  DevArr(const DevArr &) = delete;
+  DevArr &operator=(const DevArr &) = delete;
+  std::vector<T> get(size_t n) const {
+    std::vector<T> v(n);
+    if (n) C2G_CUDA(cudaMemcpy(v.data(), p, sizeof(T) * n, cudaMemcpyDeviceToHost));
+    return v;
+  }
+};
+
+// Traces the paths (start x, iup, path length from pathini) to their ends on
+// the device; returns the field evaluations made.
+long trace_paths_dev(Handle &h, std::vector<Path> &paths, const std::vector<double> &pathini, int ncp,
+                     const double *cpx, const int *cptyp) {
+  const int n = (int)paths.size();
+  if (n == 0) return 0;
+  const HostWfn &w = h.host;
+  std::vector<double> x0(3 * (size_t)n);
+  std::vector<int> iup(n);
+  for (int i = 0; i < n; i++) {
+    for (int k = 0; k < 3; k++) x0[3 * i + k] = paths[i].x[k];
+    iup[i] = paths[i].iup;
+  }
+  DevArr<double> dx0(x0), dpi(pathini), dcp(std::vector<double>(cpx, cpx + 3 * (size_t)ncp)), dxyz(w.xyz);
+  DevArr<int> diup(iup), dtyp(std::vector<int>(cptyp, cptyp + ncp)), dz(w.z);
+  DevArr<double> dxe(3 * (size_t)n), dpl(n);
+  DevArr<int> dier(n), dns(n);
+  DevArr<long> dev(n);
+  PathGeom g = host_geom(w);
+  g.xyz = dxyz.p;
+  g.z = dz.p;
+  PathsDev d{n, dx0.p, dpi.p, diup.p, ncp, dcp.p, dtyp.p, dxe.p, dpl.p, dier.p, dns.p, dev.p};
+  int dev_id = 0, sms = 0;
+  C2G_CUDA(cudaGetDevice(&dev_id));
+  C2G_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+  launch_trace_paths(h.dev, g, d, std::min(n, 3 * sms), 0);
+  C2G_CUDA(cudaDeviceSynchronize());
+  const std::vector<double> xe = dxe.get(3 * (size_t)n), pl = dpl.get(n);
+  const std::vector<int> ie = dier.get(n), ns = dns.get(n);
+  const std::vector<long> ev = dev.get(n);
+  long nev = 0;
+  for (int i = 0; i < n; i++) {
+    for (int k = 0; k < 3; k++) paths[i].x[k] = xe[3 * i + k];
+    paths[i].ier = ie[i], paths[i].nstep = ns[i], paths[i].plen = pl[i];
+    nev += ev[i];
+  }
+  return nev;
+}
 
 // Symmetric 3x3 eigen-decomposition (column-major input): cyclic Jacobi,
 // eigenvalues ascending, vec + 3 j = eigenvector j, each scaled so that its
@@ -121,6 +183,7 @@ int c2g_cp_graph(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *cp_typ, 
     }
     const int nb = (int)bcp.size();
     BatchGrd bg(h, std::max(2 * nb, 1));
+    long path_evals = 0;
     std::vector<Path> paths(2 * (size_t)nb);
     if (nb > 0) {
       // Hessians at the bond and ring CPs, eigenvector of the unique
@@ -154,7 +217,11 @@ int c2g_cp_graph(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *cp_typ, 
           p.plen = std::sqrt(d2);  // pathini = the CP
         }
       }
-      trace_paths(h, paths, ncp, cp_xyz, cp_typ, bg);
+      std::vector<double> pathini(6 * (size_t)nb);
+      for (int b = 0; b < nb; b++)
+        for (int j = 0; j < 2; j++)
+          for (int k = 0; k < 3; k++) pathini[3 * (2 * b + j) + k] = cp_xyz[3 * bcp[b] + k];
+      path_evals = trace_paths_dev(h, paths, pathini, ncp, cp_xyz, cp_typ);
     }
     // end points -> terminating CPs, distances, angle (makegraph :2196-2262)
     for (int b = 0; b < nb; b++) {
@@ -200,8 +267,8 @@ int c2g_cp_graph(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *cp_typ, 
     }
     if (stats) {
       stats->npath = 2 * nb;
-      stats->nbatch = (int)bg.launches();
-      stats->nevals = bg.evals();
+      stats->nbatch = (int)bg.launches() + (nb > 0 ? 1 : 0);
+      stats->nevals = bg.evals() + path_evals;
       stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
   });

@@ -1,7 +1,8 @@
-// The zero-flux surface search of critic2's INTEGRALS on the GPU, every ray
-// resident on the device: bisect_msurface (src/bisect@proc.f90:1208-1446)
-// and lim_surf (:1039-1126) for one (attractor, angular node) per block at
-// a time, over field%gradient's paths (gpath.h).
+// Gradient paths resident on the GPU: the zero-flux surface search of
+// critic2's INTEGRALS, bisect_msurface (src/bisect@proc.f90:1208-1446) and
+// lim_surf (:1039-1126) for one (attractor, angular node) per block at a
+// time, and makegraph's single paths (src/autocp@proc.f90:2116-2268), one
+// per block, both over field%gradient's paths (gpath.h).
 //
 // Thread 0 of a block runs the ray's state machine (bracket tries, the
 // bisection, beta-sphere restarts, and the path's Bogacki-Shampine steps);
@@ -25,7 +26,7 @@
 #include "c2g_internal.h"
 #include "gpath.h"
 #include "gto.cuh"
-#include "k_basin.h"
+#include "k_gpath.h"
 #include "points.cuh"
 
 namespace c2g {
@@ -419,7 +420,67 @@ __global__ void __launch_bounds__(256) k_basin_rays(DevWfn w, PathGeom g, BasinD
   }
 }
 
+// Single gradient paths (makegraph's), one block per path at a time: thread
+// 0 steps the path, the block evaluates the field it asks for.
+template <int MPT>
+__global__ void __launch_bounds__(256) k_trace_paths(DevWfn w, PathGeom g, PathsDev d) {
+  __shared__ double s_chi[256 * 4];
+  __shared__ int s_k[256];
+  __shared__ int s_wn[8];
+  __shared__ double s_red[8 * 4 + 4];
+  __shared__ double s_x[3];
+  __shared__ int s_more;
+  __shared__ __align__(16) unsigned char s_path[sizeof(Path)];
+  Path &p = *reinterpret_cast<Path *>(s_path);
+  for (int i = blockIdx.x; i < d.n; i += gridDim.x) {
+    long nev = 0;
+    if (threadIdx.x == 0) start_path(p, d.x0 + 3 * i, d.iup[i], d.pathini + 3 * i);
+    for (;;) {
+      if (threadIdx.x == 0) {
+        bool need = p.stage == -1;
+        while (!need && !p.done) {
+          if (p.stage == 0 && !head(p, g, d.ncp, d.cpx, d.cptyp, nullptr)) {
+            p.done = true;
+            break;
+          }
+          if (p.stage == 0) request_stage1(p);
+          need = true;
+        }
+        if (need && nev >= kMaxRayEvals) need = false, p.ier = 2, p.done = true;
+        s_more = need ? 1 : 0;
+        if (need) s_x[0] = p.req[0], s_x[1] = p.req[1], s_x[2] = p.req[2];
+      }
+      __syncthreads();
+      if (!s_more) break;
+      const double xx[3] = {s_x[0], s_x[1], s_x[2]};
+      double q[4];
+      eval_block<MPT>(w, xx, s_chi, s_k, s_wn, s_red, q);
+      if (threadIdx.x == 0) {
+        nev++;
+        if (p.stage == -1) take_start(p, q);
+        else advance(p, q);
+      }
+    }
+    if (threadIdx.x == 0) {
+      if (p.incstep) p.nstep++;
+      for (int j = 0; j < 3; j++) d.xend[3 * i + j] = p.x[j];
+      d.ier[i] = p.ier;
+      d.nstep[i] = p.nstep;
+      d.plen[i] = p.plen;
+      d.nevals[i] = nev;
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
+
+void launch_trace_paths(const DevWfn &w, const PathGeom &g, const PathsDev &d, int grid, cudaStream_t st) {
+  if (w.nmo <= 256) k_trace_paths<1><<<grid, 256, 0, st>>>(w, g, d);
+  else if (w.nmo <= 512) k_trace_paths<2><<<grid, 256, 0, st>>>(w, g, d);
+  else k_trace_paths<4><<<grid, 256, 0, st>>>(w, g, d);
+  C2G_CUDA(cudaGetLastError());
+}
 
 void launch_basin_rays(const DevWfn &w, const PathGeom &g, const BasinDev &b, int grid, cudaStream_t st) {
   if (w.nmo <= 256) k_basin_rays<1><<<grid, 256, 0, st>>>(w, g, b);

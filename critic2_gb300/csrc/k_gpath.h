@@ -1,4 +1,5 @@
-// Device side of the basin-integral surface search (k_basin.cu).
+// Device-resident gradient paths (k_gpath.cu): the basin-integral surface
+// search and makegraph's single paths.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,6 +26,23 @@ struct BasinDev {
   int *ray_npath, *ray_nwarn, *ray_nrestart, *ray_err;  // err: 1 no bracket, 2 restarts, 3 evaluations
   long *ray_nevals;
 };
+
+// n single paths from x0 (3 * n) going iup (+1 up, -1 down), path length
+// counted from pathini, with the default beta spheres; end point, ier,
+// step count, length and evaluations per path.
+struct PathsDev {
+  int n;
+  const double *x0, *pathini;
+  const int *iup;
+  int ncp;
+  const double *cpx;
+  const int *cptyp;
+  double *xend, *plen;
+  int *ier, *nstep;
+  long *nevals;
+};
+
+void launch_trace_paths(const DevWfn &w, const gpath::PathGeom &g, const PathsDev &d, int grid, cudaStream_t st);
 
 // Every ray of the search, one block of 256 threads per ray at a time.
 void launch_basin_rays(const DevWfn &w, const gpath::PathGeom &g, const BasinDev &b, int grid, cudaStream_t st);

@@ -440,13 +440,13 @@ int c2g_autocritic(c2g_wfn *h, int nseed, const double *xseed, int prec, int max
  *   brang(ncp)       angle (degrees) between the two end vectors
  *   brvec(3,ncp)     the unit eigenvector e
  *   ier(2,ncp), nstep(2,ncp)   field%gradient's ier and step count (may be NULL)
- * The paths are traced together, one GPU batch of FP64 evaluations per
- * Runge-Kutta stage.  The sign of e follows a fixed rule (largest
+ * The paths are traced on the GPU, one block per path (the steps and their
+ * FP64 evaluations on the device).  The sign of e follows a fixed rule (largest
  * component positive), not LAPACK's, so the two paths of a CP may be
  * listed in the other order than critic2 lists them. */
 typedef struct {
   int npath;       /* gradient paths traced */
-  int nbatch;      /* GPU evaluation batches */
+  int nbatch;      /* GPU launches (Hessians at the CPs, the paths) */
   long nevals;     /* field evaluations */
   double ms_total; /* wall time of the call */
 } c2g_graph_stats;
@@ -497,7 +497,7 @@ typedef struct {
   int natt;        /* attractors integrated */
   int nray;        /* rays per attractor */
   long npath;      /* gradient paths traced */
-  long nbatch;     /* GPU evaluation batches of the surface search */
+  long nbatch;     /* GPU launches of the surface search */
   long nevals;     /* field evaluations (paths and quadrature) */
   int nwarn;       /* paths that ended with field%gradient's ier > 0 */
   int nrestart;    /* beta-sphere shrinks (bisection restarts) */
