@@ -138,9 +138,11 @@ static_assert(CBUF0 + NCBUF * 16 <= (int)TMEM_COLS, "TMEM budget");
 constexpr int RED = 81;  // padded row of the reduction buffer
 constexpr int TAB = 4 * 13;  // axis-factor table: 4 primitives x (1 x + 4 y + 8 z values)
 // barrier slots
-// (the epilogue's partial sums are double-buffered: EPIFULL / EPIFREE per buffer)
-constexpr int B_CHI = 0, B_C = 6, B_EMPTY = 10, B_ACCFULL = 16, B_ACCEMPTY = 17, B_EPIFULL = 18,
-              B_EPIFREE = 20, B_TREADY = 22, B_TFREE = 24, B_DRAIN = 26, NBAR = 27;
+// (B_CHI + stage buffer: the stage's basis block and its coefficients are in
+// place, one arrival by the producer warp and one by each loader warp; the
+// epilogue's partial sums are double-buffered: EPIFULL / EPIFREE per buffer)
+constexpr int B_CHI = 0, B_EMPTY = 6, B_ACCFULL = 12, B_ACCEMPTY = 13, B_EPIFULL = 14, B_EPIFREE = 16,
+              B_TREADY = 18, B_TFREE = 20, B_DRAIN = 22, NBAR = 23;
 // One producer warp per stage buffer.  The buffer waits are mbarrier parity
 // waits; with more producers than buffers the producer of stage g could wait
 // for stage g - NSTAGE while stage g - 2 NSTAGE still holds the buffer, and
@@ -895,10 +897,9 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
 
   if (threadIdx.x == 0) {
     for (int b = 0; b < K::NSTAGE; b++) {
-      ptx::mbar_init(&s.bar[K::B_CHI + b], 1);
+      ptx::mbar_init(&s.bar[K::B_CHI + b], 1 + 4);  // the producer and the four loaders
       ptx::mbar_init(&s.bar[K::B_EMPTY + b], 1);
     }
-    for (int b = 0; b < K::NCBUF; b++) ptx::mbar_init(&s.bar[K::B_C + b], 4);
     ptx::mbar_init(&s.bar[K::B_ACCFULL], 1);
     ptx::mbar_init(&s.bar[K::B_ACCEMPTY], 4);
     for (int p = 0; p < 2; p++) {
@@ -1096,7 +1097,6 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           for (int j = 0; j < nact; j++, g++) {
             const int b = g % K::NSTAGE, cb = g % K::NCBUF;
             if (!(ok = thread_wait(s, K::B_CHI + b, (g / K::NSTAGE) & 1, a.err))) break;
-            if (!(ok = thread_wait(s, K::B_C + cb, (g / K::NCBUF) & 1, a.err))) break;
             ptx::tc_fence_after();
             const uint32_t a_hi = tmem + K::CBUF0 + cb * 16, a_lo = a_hi + 8;
             const uint32_t sb = ptx::smem_u32(s.stage + b * K::STAGE);
@@ -1219,7 +1219,8 @@ __global__ void __launch_bounds__(K::NTHR, 1) k_tc(TcArgs a, Src src, Sink sink,
           ptx::tmem_wait_st();
           ptx::tc_fence_before();
           __syncwarp();
-          if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_C + cb]);
+          // stage g's coefficients are in TMEM buffer cb
+          if (lane == 0) ptx::mbar_arrive(&s.bar[K::B_CHI + g % K::NSTAGE]);
         }
         if (!ok) break;
         // ----- epilogue of this (point tile, MO tile)
