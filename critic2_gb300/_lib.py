@@ -23,7 +23,7 @@ EXPORTS = ("c2g_abi_version", "c2g_last_error", "c2g_wfn_create", "c2g_wfn_read_
            "c2g_nciplot_dev", "c2g_nciplot_dev_noalloc", "c2g_newton", "c2g_pair_seeds",
            "c2g_autocritic", "c2g_nci_post_dev", "c2g_cube_text", "c2g_dat_text", "c2g_nciplot_files",
            "c2g_grid_field_dev", "c2g_cube_precise_text", "c2g_cube_field_file",
-           "c2g_nci_chk_write", "c2g_nci_chk_read", "c2g_cp_graph", "c2g_basin_size", "c2g_basin_integrals",
+           "c2g_nci_chk_write", "c2g_nci_chk_read", "c2g_cp_graph", "c2g_basin_size", "c2g_basin_integrals", "c2g_sphere_integrals",
            "c2g_mesh_size", "c2g_mesh_dev", "c2g_molcalc",
            # learned CP-seed proposer (include/critic2_gb300_cpseed.h)
            "c2g_cs_conv3d", "c2g_cs_conv3d_bwd_data", "c2g_cs_conv3d_bwd_weight", "c2g_cs_loss",
@@ -96,6 +96,8 @@ def lib():
     L.c2g_cp_graph.argtypes = [_vp, C.c_int, _vp, _vp] + [_vp] * 7 + [C.POINTER(GraphStats)]
     L.c2g_basin_size.argtypes = [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)]
+    L.c2g_sphere_integrals.argtypes = [_vp, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, C.c_double, _vp, _vp, _vp]
     L.c2g_basin_integrals.argtypes = [_vp, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double] + \
         [_vp] * 6 + [C.POINTER(BasinStats)]
     L.c2g_nci_chk_write.argtypes = [C.c_char_p, _dp, _dp, _ip, _dp, _dp]

@@ -480,4 +480,100 @@ int c2g_basin_integrals(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *c
   });
 }
 
+// SPHEREINTEGRALS (src/bisect@proc.f90:573-784): for each attractor, Pop
+// and Lap inside spheres of nr radii r0 exp(h (n - 1)) up to rend (rend < 0:
+// |rend| times half the distance to the nearest atom, get_rnn2), each
+// sphere by sphereintegrals_lebedev / _gauleg (:793-854): the angular rule
+// times 50 radial Gauss-Legendre nodes on (0, r), summed as lebedev_mquad /
+// gauleg_mquad.
+int c2g_sphere_integrals(c2g_wfn *hp, int ncp, const double *cp_xyz, const int *cp_typ, int meth, int n1, int n2,
+                         int cpid, int nr, double r0, double rend, int *att_cp, double *radii, double *props) {
+  return guarded([&] {
+    if (!hp) fail(C2G_ERR_ARG, "null handle");
+    Handle &hd = *reinterpret_cast<Handle *>(hp);
+    const HostWfn &w = hd.host;
+    if (ncp < 0 || (ncp > 0 && (!cp_xyz || !cp_typ))) fail(C2G_ERR_ARG, "bad CP list");
+    if (!props || !radii) fail(C2G_ERR_ARG, "null output");
+    if (nr < 1) fail(C2G_ERR_ARG, "nr must be positive");
+    if (!(r0 > 0.0)) fail(C2G_ERR_ARG, "r0 must be positive");
+    DeviceGuard guard(hd.device);
+    std::vector<double> cpx(cp_xyz, cp_xyz + 3 * (size_t)ncp);
+    std::vector<int> typ(cp_typ, cp_typ + ncp);
+    if (ncp == 0) {
+      cpx = w.xyz;
+      typ.assign(w.natom, -3);
+    }
+    const int nc = (int)typ.size();
+    check_cp_list(w, nc, cpx.data(), typ.data());
+    if (cpid < 0 || cpid > nc) fail(C2G_ERR_ARG, "cpid out of range");
+    std::vector<Node> nodes;
+    std::vector<double> lw;
+    std::vector<int> ring;
+    if (meth == C2G_INT_LEBEDEV) lebedev_nodes(ray_count(meth, n1, n2), nodes, lw);
+    else if (meth == C2G_INT_GAULEG) gauleg_nodes(n1, n2, nodes, ring);
+    else fail(C2G_ERR_ARG, "unknown integration method");
+    const int nray = (int)nodes.size();
+    std::vector<double> tp, tw;
+    if (meth == C2G_INT_GAULEG) gauleg(0.0, M_PI, n1, tp, tw);
+    const std::vector<int> ai = attractor_list(w, nc, typ.data(), cpid);
+    for (size_t a = 0; a < ai.size(); a++) {
+      const double *xa = cpx.data() + 3 * ai[a];
+      // get_rnn2: half the distance to the nearest atom (0 for a lone atom)
+      double rnn = kVBig;
+      for (int b = 0; b < w.natom; b++) {
+        double d2 = 0.0;
+        for (int j = 0; j < 3; j++) d2 += (w.xyz[3 * b + j] - xa[j]) * (w.xyz[3 * b + j] - xa[j]);
+        if (d2 > 0.0) rnn = std::min(rnn, std::sqrt(d2));
+      }
+      const double rnn2 = w.natom <= 1 ? 0.0 : 0.5 * rnn;
+      const double lh = nr > 1 ? std::log((rend < 0.0 ? rnn2 * std::fabs(rend) : rend) / r0) / (nr - 1) : 0.0;
+      std::vector<double> xyz, rr((size_t)nr * kRadNodes), rw((size_t)nr * kRadNodes);
+      xyz.reserve(3 * (size_t)nr * nray * kRadNodes);
+      for (int n = 0; n < nr; n++) {
+        const double rad = nr == 1 ? (rend < 0.0 ? rnn2 * std::fabs(rend) : r0) : r0 * std::exp(n * lh);
+        radii[a * (size_t)nr + n] = rad;
+        std::vector<double> gr, gw;
+        gauleg(0.0, rad, kRadNodes, gr, gw);
+        std::copy(gr.begin(), gr.end(), rr.begin() + (size_t)n * kRadNodes);
+        std::copy(gw.begin(), gw.end(), rw.begin() + (size_t)n * kRadNodes);
+        for (int i = 0; i < nray; i++)
+          for (int k = 0; k < kRadNodes; k++)
+            for (int j = 0; j < 3; j++) xyz.push_back(xa[j] + gr[k] * nodes[i].u[j]);
+      }
+      std::vector<double> prop;
+      eval_props(hd, xyz, prop);
+      size_t ip = 0;
+      for (int n = 0; n < nr; n++) {
+        const double *gr = rr.data() + (size_t)n * kRadNodes, *gw = rw.data() + (size_t)n * kRadNodes;
+        std::vector<double> rp(kNProp * (size_t)nray);
+        for (int i = 0; i < nray; i++) {
+          double acc[kNProp] = {0, 0};
+          for (int k = 0; k < kRadNodes; k++, ip++)
+            for (int q = 0; q < kNProp; q++) acc[q] += gr[k] * gr[k] * gw[k] * prop[kNProp * ip + q];
+          for (int q = 0; q < kNProp; q++) rp[kNProp * i + q] = acc[q];
+        }
+        double sp[kNProp] = {0, 0};
+        if (meth == C2G_INT_LEBEDEV) {
+          for (int i = 0; i < nray; i++)
+            for (int q = 0; q < kNProp; q++) sp[q] += rp[kNProp * i + q] * lw[i];
+        } else {
+          std::vector<double> pp, pw;
+          int v = 0;
+          for (int t = 0; t < n1; t++) {
+            const int np = (int)(n2 * std::fabs(std::sin(tp[t]))) + 1;
+            gauleg(0.0, 2.0 * M_PI, np, pp, pw);
+            double pr[kNProp] = {0, 0};
+            for (int k = 0; k < np; k++, v++)
+              for (int q = 0; q < kNProp; q++) pr[q] += rp[kNProp * v + q] * pw[k];
+            const double f = std::sin(nodes[v - 1].th) * tw[t];
+            for (int q = 0; q < kNProp; q++) sp[q] += f * pr[q];
+          }
+        }
+        for (int q = 0; q < kNProp; q++) props[(a * (size_t)nr + n) * kNProp + q] = sp[q];
+      }
+      if (att_cp) att_cp[a] = ai[a];
+    }
+  });
+}
+
 }  // extern "C"

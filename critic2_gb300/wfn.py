@@ -314,6 +314,27 @@ class Wavefunction:
                           nwarn=st.nwarn, nrestart=st.nrestart, ms=st.ms_total)
         return o
 
+    def sphere_integrals(self, cp_xyz=None, cp_typ=None, meth: str = "gauleg", n: int = 20, nphi: int = 20,
+                         cpid: int = 0, nr: int = 100, r0: float = 1e-3, rend: float = -1.0) -> dict:
+        """Pop and Lap inside spheres around the attractors
+        (c2g_sphere_integrals; critic2's SPHEREINTEGRALS): att_cp (natt,),
+        radii (natt, nr), props (natt, nr, 2)."""
+        if cp_xyz is None:
+            x, t, ncp = None, None, 0
+        else:
+            x, t = _f64(cp_xyz).reshape(-1, 3), _i32(cp_typ)
+            ncp = t.shape[0]
+        m = {"lebedev": 0, "gauleg": 1}[meth]
+        natt, nray = C.c_int(0), C.c_int(0)
+        L.check(L.lib().c2g_basin_size(self._h, ncp, L.ptr(t), m, int(n), int(nphi), int(cpid), C.byref(natt),
+                                       C.byref(nray)))
+        na = natt.value
+        o = dict(att_cp=np.zeros(na, np.int32), radii=np.zeros((na, nr)), props=np.zeros((na, nr, 2)))
+        L.check(L.lib().c2g_sphere_integrals(self._h, ncp, L.ptr(x), L.ptr(t), m, int(n), int(nphi), int(cpid),
+                                             int(nr), float(r0), float(rend), L.ptr(o["att_cp"]), L.ptr(o["radii"]),
+                                             L.ptr(o["props"])))
+        return o
+
     def autocritic(self, seeds: Optional[np.ndarray] = None, prec="fp64") -> dict:
         s = None if seeds is None else _f64(seeds).reshape(-1, 3)
         ns = 0 if s is None else s.shape[0]

@@ -506,6 +506,19 @@ typedef struct {
 
 int c2g_basin_size(c2g_wfn *h, int ncp, const int *cp_typ, int meth, int n1, int n2, int cpid, int *natt,
                    int *nray);
+
+/* Integrals over spheres around the attractors: critic2's SPHEREINTEGRALS
+ * (src/bisect@proc.f90:573-784; SPHEREINTEGRALS GAULEG ntheta nphi |
+ * LEBEDEV n, NR nr, R0 r0, REND rend, CP id).  For each attractor (as
+ * c2g_basin_integrals selects them; natt from c2g_basin_size) Pop and Lap
+ * inside nr spheres of radius r0 exp(h (n - 1)), n = 1..nr, the last
+ * radius rend (rend < 0: |rend| times half the distance to the nearest
+ * atom, get_rnn2; critic2's defaults are nr = 100, r0 = 1e-3 bohr,
+ * rend = -1, GAULEG 20 20 or LEBEDEV 770).  Each sphere is the angular rule
+ * times 50 radial Gauss-Legendre nodes on (0, r), FP64.  Outputs:
+ * att_cp(natt) (may be NULL), radii(nr, natt), props(2, nr, natt). */
+int c2g_sphere_integrals(c2g_wfn *h, int ncp, const double *cp_xyz, const int *cp_typ, int meth, int n1, int n2,
+                         int cpid, int nr, double r0, double rend, int *att_cp, double *radii, double *props);
 int c2g_basin_integrals(c2g_wfn *h, int ncp, const double *cp_xyz, const int *cp_typ, int meth, int n1, int n2,
                         int cpid, double iasprec, int *att_cp, double *props, double *iaserr, double *rays,
                         double *rsurf, double *rbeta_int, c2g_basin_stats *stats);

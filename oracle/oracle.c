@@ -1667,3 +1667,53 @@ int o_basin_integrals(const owfn *w, int ncp, const double *cpx, const int *cpty
   if (nrestart_out) *nrestart_out = nrestart;
   return fail ? -1 : natt;
 }
+
+/* SPHEREINTEGRALS (src/bisect@proc.f90:573-784) for the attractors of the
+ * CP list (as o_basin_integrals selects them): Pop and Lap inside nr
+ * spheres of radius r0 exp(h (n - 1)), the last radius rend (rend < 0:
+ * |rend| times half the distance to the nearest atom), each by the angular
+ * rule (u, wang; ring/ringw as in o_basin_integrals) times 50 radial
+ * Gauss-Legendre nodes on (0, r).  Outputs radii(nr, natt), props(2, nr,
+ * natt), att_cp(natt).  Returns natt. */
+int o_sphere_integrals(const owfn *w, int ncp, const double *cpx, const int *cptyp, int cpid, int nray,
+                       const double *u, const double *wang, const int *ring, int nring, const double *ringw, int nr,
+                       double r0, double rend, int nthreads, int *att_cp, double *radii, double *props) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  int lo = cpid > 0 ? cpid - 1 : 0, hi = cpid > 0 ? cpid : ncp, natt = 0;
+  double *rp = malloc(sizeof(double) * 2 * (size_t)(nray > 0 ? nray : 1));
+  for (int c = lo; c < hi; c++) {
+    if (!(c < w->natom || cptyp[c] == -3)) continue;
+    const double *xa = cpx + 3 * c;
+    double rnn = DBL_MAX;
+    for (int b = 0; b < w->natom; b++) {
+      double d = dist3(w->xyz + 3 * b, xa);
+      if (d > 0.0) rnn = fmin(rnn, d);
+    }
+    double rnn2 = w->natom <= 1 ? 0.0 : 0.5 * rnn;
+    double h = nr > 1 ? log((rend < 0.0 ? rnn2 * fabs(rend) : rend) / r0) / (nr - 1) : 0.0;
+    for (int n = 0; n < nr; n++) {
+      double rad = nr == 1 ? (rend < 0.0 ? rnn2 * fabs(rend) : r0) : r0 * exp(n * h);
+      radii[(size_t)natt * nr + n] = rad;
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int i = 0; i < nray; i++) o_radialquad(w, xa, u + 3 * i, 0.0, rad, 1e-5, rp + 2 * i, NULL);
+      double sp[2] = {0, 0};
+      if (!ring) {
+        for (int i = 0; i < nray; i++) sp[0] += rp[2 * i] * wang[i], sp[1] += rp[2 * i + 1] * wang[i];
+      } else {
+        for (int t = 0; t < nring; t++) {
+          double pr[2] = {0, 0};
+          for (int i = 0; i < nray; i++)
+            if (ring[i] == t) pr[0] += rp[2 * i] * wang[i], pr[1] += rp[2 * i + 1] * wang[i];
+          sp[0] += ringw[t] * pr[0], sp[1] += ringw[t] * pr[1];
+        }
+      }
+      props[((size_t)natt * nr + n) * 2] = sp[0];
+      props[((size_t)natt * nr + n) * 2 + 1] = sp[1];
+    }
+    att_cp[natt++] = c;
+  }
+  free(rp);
+  return natt;
+}

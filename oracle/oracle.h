@@ -104,6 +104,9 @@ int o_basin_integrals(const owfn *w, int ncp, const double *cpx, const int *cpty
                       const double *usph, const double *wsph, double prec, int stats, int nthreads, int *att_cp,
                       double *props, double *iaserr, double *rsurf, double *rbeta_int, int *nwarn_out,
                       int *nrestart_out);
+int o_sphere_integrals(const owfn *w, int ncp, const double *cpx, const int *cptyp, int cpid, int nray,
+                       const double *u, const double *wang, const int *ring, int nring, const double *ringw, int nr,
+                       double r0, double rend, int nthreads, int *att_cp, double *radii, double *props);
 
 /* Molecular meshes (src/meshmod@proc.f90:79-627): type 1 Becke, 2
  * Franchini; ang(4, nang) the angular rule (weights sum to 1). */

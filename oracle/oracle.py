@@ -81,6 +81,10 @@ def lib():
                                         C.c_int, C.c_void_p, C.c_int, _dp, _dp, C.c_double, C.c_int, C.c_int,
                                         _ip, _dp, _dp, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.o_basin_integrals.restype = C.c_int
+        L.o_sphere_integrals.argtypes = [C.c_void_p, C.c_int, _dp, _ip, C.c_int, C.c_int, _dp, _dp, C.c_void_p,
+                                         C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, _ip, _dp,
+                                         _dp]
+        L.o_sphere_integrals.restype = C.c_int
         L.o_z2nr.argtypes = [C.c_int, C.c_int]
         L.o_z2nr.restype = C.c_int
         L.o_mesh_size.argtypes = [C.c_void_p, C.c_int, C.c_int]
@@ -242,6 +246,26 @@ class Wfn:
         for k in ("att_cp", "props", "iaserr", "rsurf", "rbeta_int"):
             out[k] = out[k][:got]
         out["nwarn"], out["nrestart"] = nw.value, nr.value
+        return out
+
+    def sphere_integrals(self, cp_xyz, cp_typ, u, wang, ring=None, ringw=None, cpid=0, nr=100, r0=1e-3, rend=-1.0,
+                         nthreads=0):
+        """SPHEREINTEGRALS: dict of att_cp, radii (natt, nr), props (natt, nr, 2: Pop, Lap)."""
+        ct = _i32(cp_typ)
+        n = len(ct)
+        nat = self.mol.natom
+        na = len([i for i in (range(n) if cpid <= 0 else [cpid - 1]) if i < nat or ct[i] == -3])
+        out = dict(att_cp=np.zeros(max(na, 1), np.int32), radii=np.zeros((max(na, 1), nr)),
+                   props=np.zeros((max(na, 1), nr, 2)))
+        rg = _i32(ring) if ring is not None else None
+        rw = _f64(ringw) if ringw is not None else None
+        got = lib().o_sphere_integrals(
+            self.h, n, _f64(cp_xyz).reshape(-1), ct, int(cpid), len(u), _f64(u).reshape(-1), _f64(wang),
+            rg.ctypes.data_as(C.c_void_p) if rg is not None else None, len(rw) if rw is not None else 0,
+            rw.ctypes.data_as(C.c_void_p) if rw is not None else None, int(nr), float(r0), float(rend),
+            int(nthreads), out["att_cp"], out["radii"].reshape(-1), out["props"].reshape(-1))
+        for k in ("att_cp", "radii", "props"):
+            out[k] = out[k][:got]
         return out
 
     def mesh(self, mesh="franchini", level="good", nthreads=0):

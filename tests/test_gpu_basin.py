@@ -103,3 +103,25 @@ def test_basin_arguments(gpu_lib):
     one = w.basin_integrals(None, None, "lebedev", 6, cpid=2)
     assert list(one["att_cp"]) == [1] and one["rays"].shape == (6, 3)
     assert w.basin_integrals(None, None, "lebedev", 7)["rays"].shape == (14, 3)  # good_lebedev rounds up
+
+
+def test_sphere_integrals_vs_oracle(gpu_lib, oracle_mod):
+    """SPHEREINTEGRALS through the C ABI against the oracle: nci12's first
+    nucleus (LEBEDEV 110, 6 radii up to half the nearest-neighbour distance)
+    and the diatomic's two (GAULEG 10 14)."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("nci12")
+    w, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    cpx, cpt = mol.atom_xyz.copy(), np.full(mol.natom, -3, np.int32)
+    g = w.sphere_integrals(cpx, cpt, "lebedev", 110, cpid=1, nr=6)
+    u, wu = lebedev_rays(oracle_mod, 110)
+    r = o.sphere_integrals(cpx, cpt, u, wu, cpid=1, nr=6)
+    assert list(g["att_cp"]) == [0] and np.allclose(g["radii"], r["radii"], rtol=1e-14)
+    assert np.allclose(g["props"], r["props"], rtol=1e-11, atol=1e-14)
+    mol = diatomic()
+    w, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    cpx, cpt = mol.atom_xyz.copy(), np.array([-3, -3], np.int32)
+    g = w.sphere_integrals(cpx, cpt, "gauleg", 10, nphi=14, nr=4, r0=0.05, rend=1.0)
+    gu, gw, ring, ringw = gauleg_rays(10, 14)
+    r = o.sphere_integrals(cpx, cpt, gu, gw, ring=ring, ringw=ringw, nr=4, r0=0.05, rend=1.0)
+    assert np.allclose(g["props"], r["props"], rtol=1e-11, atol=1e-14)

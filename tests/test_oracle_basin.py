@@ -176,3 +176,24 @@ def test_basin_single_cp(oracle_mod, di):
     b = w.basin_integrals(cpx, cpt, u, wu, us, ws, cpid=2)
     assert list(b["att_cp"]) == [1]
     assert np.allclose(b["props"][0], a["props"][1], rtol=1e-12)
+
+
+def test_sphere_integrals_one_center(oracle_mod):
+    """SPHEREINTEGRALS around a lone s-type center, rho = occ c^2 exp(-b r^2)
+    (b = 2 alpha): Pop = 4 pi occ c^2 int_0^R r^2 exp(-b r^2) dr (erf form)
+    and Lap = 4 pi R^2 rho'(R), the flux through the sphere."""
+    from math import erf
+    a, c, occ = 0.8, 1.3, 2.0
+    mol = synth.Molecule(np.zeros((1, 3)), np.array([6], np.int32), np.array([1], np.int32), np.ones(1, np.int32),
+                         np.array([a]), np.array([occ]), np.array([[c]]), name="one")
+    w = oracle_mod.Wfn(mol)
+    u, wu = lebedev_rays(oracle_mod, 110)
+    r = w.sphere_integrals(np.zeros((1, 3)), np.array([-3], np.int32), u, wu, nr=6, r0=0.1, rend=3.0)
+    b = 2 * a
+    for R, (pop, lap) in zip(r["radii"][0], r["props"][0]):
+        ref = 4 * np.pi * occ * c * c * (np.sqrt(np.pi) / (4 * b ** 1.5) * erf(np.sqrt(b) * R)
+                                         - R / (2 * b) * np.exp(-b * R * R))
+        rho_r = occ * c * c * np.exp(-b * R * R)
+        assert abs(pop - ref) <= 1e-10 * abs(ref)
+        assert abs(lap - 4 * np.pi * R * R * (-2 * b * R) * rho_r) <= 1e-9 * abs(4 * np.pi * R * R * 2 * b * R * rho_r)
+    assert np.allclose(r["radii"][0], 0.1 * np.exp(np.arange(6) * np.log(30.0) / 5), rtol=1e-14)
