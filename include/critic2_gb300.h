@@ -213,7 +213,8 @@ typedef struct {
  * cgrad(k,j,i) = s (k fastest), host arrays of nstep(1)*nstep(2)*nstep(3)
  * doubles.  xmat is column-major (column i = step vector of axis i).
  * In the split modes the points whose Hessian eigenvalues satisfy
- * |lambda2| < 1e-3 |lambda1| are re-evaluated in FP64.  stats may be NULL. */
+ * |lambda2| < recheck max|lambda| (C2G_PARAM_RECHECK_REL) are re-evaluated
+ * in FP64.  stats may be NULL. */
 int c2g_nciplot(c2g_wfn *h, const double *x0, const double *xmat, const int *nstep, int prec,
                 double *crho, double *cgrad, c2g_nci_stats *stats);
 
