@@ -47,16 +47,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Waits for the phase with the given parity to complete; gives up after
-// timeout_ns (returns false).
+// timeout_ns (returns false).  try_wait suspends the warp in hardware until
+// the phase completes or a short time limit passes, so polling costs few
+// issue slots; a sleep between polls only delays the wake-up on the
+// pipeline's critical chain (measured 1-5% slower), so there is none.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t timeout_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
-  uint32_t spins = 0;
-  while (!mbar_try_wait(bar, parity)) {
-    // back off so that waiting warps leave the issue slots to working ones
-    if (++spins > 4) __nanosleep(spins < 64 ? 32u : 256u);
+  while (!mbar_try_wait(bar, parity))
     if (globaltimer() - t0 > timeout_ns) return false;
-  }
   return true;
 }
 
