@@ -271,71 +271,75 @@ __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_ch
   const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
   double x[3] = {xin[0], xin[1], xin[2]};
   wrap_cell(w, x);
-  double acc[MPT][4];
+  double r[4] = {0.0, 0.0, 0.0, 0.0};
+  // MOs in chunks of 256 MPT (one chunk up to 1024 MOs; above that the
+  // primitives are evaluated again for each chunk)
+  for (int mo0 = 0; mo0 < w.nmo; mo0 += 256 * MPT) {
+    double acc[MPT][4];
 #pragma unroll
-  for (int m = 0; m < MPT; m++)
+    for (int m = 0; m < MPT; m++)
 #pragma unroll
-    for (int c = 0; c < 4; c++) acc[m][c] = 0.0;
-  for (int k0 = 0; k0 < w.npri; k0 += 256) {
-    const int ip = k0 + tid;
-    double chi[4];
-    bool in = false;
-    if (ip < w.npri) {
-      const PrimF64 pr = w.prim[ip];
-      const double4 A = w.atoms[pr.atom];
-      const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
-      const double dd = dx * dx + dy * dy + dz * dz;
-      if (dd <= A.w) {
-        const double dist = sqrt(dd);
-        if (!(dist > pr.dran)) {
-          in = true;
-          chi_eval<4>(dx, dy, dz, pr.e, pr.lpack, exp(-pr.e * (dist * dist)), chi);
+      for (int c = 0; c < 4; c++) acc[m][c] = 0.0;
+    for (int k0 = 0; k0 < w.npri; k0 += 256) {
+      const int ip = k0 + tid;
+      double chi[4];
+      bool in = false;
+      if (ip < w.npri) {
+        const PrimF64 pr = w.prim[ip];
+        const double4 A = w.atoms[pr.atom];
+        const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+        const double dd = dx * dx + dy * dy + dz * dz;
+        if (dd <= A.w) {
+          const double dist = sqrt(dd);
+          if (!(dist > pr.dran)) {
+            in = true;
+            chi_eval<4>(dx, dy, dz, pr.e, pr.lpack, exp(-pr.e * (dist * dist)), chi);
+          }
         }
       }
-    }
-    const unsigned bal = __ballot_sync(0xffffffffu, in);
-    if (lane == 0) s_wn[wp] = __popc(bal);
-    __syncthreads();
-    int base = 0, nact = 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, in);
+      if (lane == 0) s_wn[wp] = __popc(bal);
+      __syncthreads();
+      int base = 0, nact = 0;
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-      base += i < wp ? s_wn[i] : 0;
-      nact += s_wn[i];
-    }
-    if (in) {
-      const int slot = base + __popc(bal & ((1u << lane) - 1u));
-#pragma unroll
-      for (int c = 0; c < 4; c++) s_chi[slot * 4 + c] = chi[c];
-      s_k[slot] = ip;
-    }
-    __syncthreads();
-    // threads without an MO skip the contraction (their sums stay zero)
-#pragma unroll 2
-    for (int j = 0; j < (tid < w.nmo ? nact : 0); j++) {
-      const double *crow = w.cmo + (size_t)s_k[j] * w.nmo_pad;
-      double ch[4];
-#pragma unroll
-      for (int c = 0; c < 4; c++) ch[c] = s_chi[j * 4 + c];
-#pragma unroll
-      for (int m = 0; m < MPT; m++) {
-        const int mo = tid + 256 * m;
-        const double cm = mo < w.nmo ? __ldg(crow + mo) : 0.0;
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[m][c] = fma(cm, ch[c], acc[m][c]);
+      for (int i = 0; i < 8; i++) {
+        base += i < wp ? s_wn[i] : 0;
+        nact += s_wn[i];
       }
-    }
-    __syncthreads();
-  }
-  double r[4] = {0.0, 0.0, 0.0, 0.0};
+      if (in) {
+        const int slot = base + __popc(bal & ((1u << lane) - 1u));
 #pragma unroll
-  for (int m = 0; m < MPT; m++) {
-    const int mo = tid + 256 * m;
-    const double o = mo < w.nmo ? w.occ[mo] : 0.0;
-    const double p0 = acc[m][0];
-    r[0] += o * p0 * p0;
-    r[1] += 2.0 * o * p0 * acc[m][1];
-    r[2] += 2.0 * o * p0 * acc[m][2];
-    r[3] += 2.0 * o * p0 * acc[m][3];
+        for (int c = 0; c < 4; c++) s_chi[slot * 4 + c] = chi[c];
+        s_k[slot] = ip;
+      }
+      __syncthreads();
+      // threads without an MO skip the contraction (their sums stay zero)
+#pragma unroll 2
+      for (int j = 0; j < (mo0 + tid < w.nmo ? nact : 0); j++) {
+        const double *crow = w.cmo + (size_t)s_k[j] * w.nmo_pad;
+        double ch[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) ch[c] = s_chi[j * 4 + c];
+#pragma unroll
+        for (int m = 0; m < MPT; m++) {
+          const int mo = mo0 + tid + 256 * m;
+          const double cm = mo < w.nmo ? __ldg(crow + mo) : 0.0;
+#pragma unroll
+          for (int c = 0; c < 4; c++) acc[m][c] = fma(cm, ch[c], acc[m][c]);
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int m = 0; m < MPT; m++) {
+      const int mo = mo0 + tid + 256 * m;
+      const double o = mo < w.nmo ? w.occ[mo] : 0.0;
+      const double p0 = acc[m][0];
+      r[0] += o * p0 * p0;
+      r[1] += 2.0 * o * p0 * acc[m][1];
+      r[2] += 2.0 * o * p0 * acc[m][2];
+      r[3] += 2.0 * o * p0 * acc[m][3];
+    }
   }
 #pragma unroll
   for (int c = 0; c < 4; c++)

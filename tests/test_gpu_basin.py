@@ -125,3 +125,23 @@ def test_sphere_integrals_vs_oracle(gpu_lib, oracle_mod):
     gu, gw, ring, ringw = gauleg_rays(10, 14)
     r = o.sphere_integrals(cpx, cpt, gu, gw, ring=ring, ringw=ringw, nr=4, r0=0.05, rend=1.0)
     assert np.allclose(g["props"], r["props"], rtol=1e-11, atol=1e-14)
+
+
+def test_basin_more_than_1024_mos(gpu_lib, oracle_mod):
+    """The device path kernels evaluate the field in chunks of 1024 MOs: a
+    1100-MO wavefunction (nci12's MOs repeated with distinct scales) gives
+    the oracle's surfaces and populations."""
+    from critic2_gb300.wfn import Wavefunction
+    base = synth.make_molecule("nci12")
+    nmo = 1100
+    cols = np.arange(nmo) % base.nmo
+    cmo = base.cmo[:, cols] * (1.0 + 1e-3 * np.arange(nmo))[None, :]
+    mol = synth.Molecule(base.atom_xyz, base.atom_z, base.icenter, base.itype, base.e,
+                         np.full(nmo, 2.0 * base.nmo / nmo), np.ascontiguousarray(cmo), name="nci12-1100")
+    w, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    g = w.basin_integrals(None, None, "lebedev", 6, cpid=1)
+    wu = matched_weights(oracle_mod, g["rays"], 6)
+    us, ws = lebedev_rays(oracle_mod, 170)
+    r = o.basin_integrals(mol.atom_xyz, np.full(mol.natom, -3, np.int32), g["rays"], wu, us, ws, cpid=1)
+    assert np.max(np.abs(g["rsurf"] - r["rsurf"])) < 1e-9
+    assert np.allclose(g["props"], r["props"], rtol=1e-9, atol=1e-12)
