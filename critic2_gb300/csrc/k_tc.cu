@@ -112,8 +112,9 @@ constexpr int NP = 32;     // points per tile
 constexpr int MT = 128;    // MOs per tile (MMA M)
 constexpr int NCOMP = 10;  // value, 3 first, 6 second derivatives
 // The B operand has one row per (component, point) of the 32-point tile:
-// row = component * 32 + point, 320 rows, so that a K-step takes six MMAs
-// with N = 64-256 (small-N MMAs run at a fraction of the tensor pipe's rate).
+// row = component * 32 + point, 320 rows, so that an MMA covers several
+// components at once (N = 32-256; small-N MMAs run at a fraction of the
+// tensor pipe's rate).
 constexpr int BROWS = NCOMP * NP;       // 320 B rows
 constexpr int BPIECE = BROWS * 32;      // 10240 bytes: one (hi|lo) B operand
 constexpr int STAGE = 2 * BPIECE;       // bytes of one K-stage (20480)
