@@ -178,33 +178,36 @@ C2G_HD inline bool head(Path &p, const PathGeom &w, int ncp, const double *cpx, 
   double d2 = 0.0;
   for (int j = 0; j < 3; j++) d2 += (p.x[j] - p.xlast[j]) * (p.x[j] - p.xlast[j]);
   p.plen += sqrt(d2);
+  // nearest nucleus, then nearer CPs of the attracting kind, by squared
+  // distances (one square root, of the minimum: the same value)
   int idnuc = 0;
-  double sphrad = 1e30;
+  double sph2 = 1e60;
   for (int a = 0; a < w.natom; a++) {
     const double dx = p.x[0] - w.xyz[3 * a], dy = p.x[1] - w.xyz[3 * a + 1], dz = p.x[2] - w.xyz[3 * a + 2];
-    const double d = sqrt(dx * dx + dy * dy + dz * dz);
-    if (d < sphrad) sphrad = d, idnuc = a;
+    const double d2a = dx * dx + dy * dy + dz * dz;
+    if (d2a < sph2) sph2 = d2a, idnuc = a;
   }
   bool have = false;
   int idcp = -1;
-  double cprad = 1e15, xcp[3] = {0, 0, 0};
+  double cp2 = 1e30, xcp[3] = {0, 0, 0};
   if (p.iup == 1 && w.z[idnuc] != 1) {
     have = true;
     idcp = idnuc;
-    cprad = sphrad;
+    cp2 = sph2;
     for (int j = 0; j < 3; j++) xcp[j] = w.xyz[3 * idnuc + j];
   }
   for (int i = 0; i < ncp; i++) {
     if (!((cptyp[i] == -3 && p.iup == 1) || (cptyp[i] == 3 && p.iup == -1))) continue;
     const double dx = p.x[0] - cpx[3 * i], dy = p.x[1] - cpx[3 * i + 1], dz = p.x[2] - cpx[3 * i + 2];
-    const double d = sqrt(dx * dx + dy * dy + dz * dz);
-    if (d < cprad) {
+    const double d2i = dx * dx + dy * dy + dz * dz;
+    if (d2i < cp2) {
       have = true;
       idcp = i;
-      cprad = d;
+      cp2 = d2i;
       for (int j = 0; j < 3; j++) xcp[j] = cpx[3 * i + j];
     }
   }
+  const double cprad = sqrt(cp2);
   if (have && cprad <= (rbeta ? rbeta[idcp] : kRBeta)) {
     p.incstep = true;
     double e2 = 0.0;
