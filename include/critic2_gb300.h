@@ -242,8 +242,9 @@ int c2g_nciplot_dev(c2g_wfn *h, const double *x0, const double *xmat, const int 
  *     allocating entry (e.g. c2g_nciplot_dev on a 1-point grid); otherwise
  *     the call returns C2G_ERR_UNSUPPORTED.  C2G_PREC_FP64 needs nothing.
  *   - The first call on each device looks up the scratch array's address
- *     (cudaGetSymbolAddress, with that device current); make that first
- *     call before any stream capture.  That first call (like the first call
+ *     (cudaGetSymbolAddress, with that device current).  Every call reads
+ *     the kernels' error word back and synchronises its stream, so no call
+ *     can be captured into a CUDA graph.  That first call (like the first call
  *     of any entry, with CUDA's default lazy module loading) also loads the
  *     library's GPU code together with the 4 MiB static array, which takes
  *     device memory once: make it before a pool of the caller's reserves
