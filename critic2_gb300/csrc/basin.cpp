@@ -221,6 +221,9 @@ SearchOut search_surfaces(Handle &h, int nc, const std::vector<double> &cpx, con
   }
   keep.emplace_back(sizeof(long) * std::max(nr, 1L));
   b.ray_nevals = keep.back().as<long>();
+  keep.emplace_back(sizeof(unsigned long long));
+  b.ray_next = keep.back().as<unsigned long long>();
+  C2G_CUDA(cudaMemset(b.ray_next, 0, sizeof(unsigned long long)));
   SearchOut out;
   if (nr > 0) {
     launch_basin_rays(h.dev, g, b, grid, 0);

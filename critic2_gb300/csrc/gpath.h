@@ -162,14 +162,50 @@ C2G_HD inline void unit(const double *q, double g[3]) {
   for (int j = 0; j < 3; j++) g[j] = q[1 + j] / (m + kVSmall);
 }
 
+// The beta-sphere candidate of head(): the nearest nucleus, then the CPs of
+// the kind the path goes to (maxima up, minima down) when nearer, with the
+// nucleus as the first candidate if the path goes up and it is not hydrogen.
+// Squared distances are compared (the square root of the minimum is the
+// same value); ties keep the first candidate.
+struct Nearest {
+  double x[3];  // the point it was found for
+  bool have;    // a candidate exists
+  bool isnuc;   // the candidate is nucleus idcp (else CP idcp)
+  int idcp;
+  double cp2;   // its squared distance
+};
+
+C2G_HD inline void nearest_serial(const double x[3], int iup, const PathGeom &w, int ncp, const double *cpx,
+                                  const int *cptyp, Nearest &n) {
+  int idnuc = 0;
+  double sph2 = 1e60;
+  for (int a = 0; a < w.natom; a++) {
+    const double dx = x[0] - w.xyz[3 * a], dy = x[1] - w.xyz[3 * a + 1], dz = x[2] - w.xyz[3 * a + 2];
+    const double d2a = dx * dx + dy * dy + dz * dz;
+    if (d2a < sph2) sph2 = d2a, idnuc = a;
+  }
+  for (int j = 0; j < 3; j++) n.x[j] = x[j];
+  n.have = n.isnuc = false;
+  n.idcp = -1;
+  n.cp2 = 1e30;
+  if (iup == 1 && w.z[idnuc] != 1) n.have = n.isnuc = true, n.idcp = idnuc, n.cp2 = sph2;
+  for (int i = 0; i < ncp; i++) {
+    if (!((cptyp[i] == -3 && iup == 1) || (cptyp[i] == 3 && iup == -1))) continue;
+    const double dx = x[0] - cpx[3 * i], dy = x[1] - cpx[3 * i + 1], dz = x[2] - cpx[3 * i + 2];
+    const double d2i = dx * dx + dy * dy + dz * dz;
+    if (d2i < n.cp2) n.have = true, n.isnuc = false, n.idcp = i, n.cp2 = d2i;
+  }
+}
+
 // The part of one field%gradient iteration before the step
 // (src/fieldmod@proc.f90:2582-2680): path length, beta spheres, molecular
 // cell, new CP.  Returns true when the path goes on with a step.  rbeta:
 // null for the default sphere (min(Rbetadef, |hini| / 2) = 0.1 bohr), or
 // per-CP radii (up2beta; the CP list then starts with the nuclei in atom
-// order, so that a nucleus found first is CP idnuc).
+// order, so that a nucleus found first is CP idnuc).  pre: the candidate
+// already found for the path's position (by a warp on the device), or null.
 C2G_HD inline bool head(Path &p, const PathGeom &w, int ncp, const double *cpx, const int *cptyp,
-                        const double *rbeta = nullptr) {
+                        const double *rbeta = nullptr, const Nearest *pre = nullptr) {
   if (p.nstep > p.mstep) {
     p.nstep = p.mstep;
     p.ier = 2;
@@ -178,35 +214,15 @@ C2G_HD inline bool head(Path &p, const PathGeom &w, int ncp, const double *cpx, 
   double d2 = 0.0;
   for (int j = 0; j < 3; j++) d2 += (p.x[j] - p.xlast[j]) * (p.x[j] - p.xlast[j]);
   p.plen += sqrt(d2);
-  // nearest nucleus, then nearer CPs of the attracting kind, by squared
-  // distances (one square root, of the minimum: the same value)
-  int idnuc = 0;
-  double sph2 = 1e60;
-  for (int a = 0; a < w.natom; a++) {
-    const double dx = p.x[0] - w.xyz[3 * a], dy = p.x[1] - w.xyz[3 * a + 1], dz = p.x[2] - w.xyz[3 * a + 2];
-    const double d2a = dx * dx + dy * dy + dz * dz;
-    if (d2a < sph2) sph2 = d2a, idnuc = a;
-  }
-  bool have = false;
-  int idcp = -1;
-  double cp2 = 1e30, xcp[3] = {0, 0, 0};
-  if (p.iup == 1 && w.z[idnuc] != 1) {
-    have = true;
-    idcp = idnuc;
-    cp2 = sph2;
-    for (int j = 0; j < 3; j++) xcp[j] = w.xyz[3 * idnuc + j];
-  }
-  for (int i = 0; i < ncp; i++) {
-    if (!((cptyp[i] == -3 && p.iup == 1) || (cptyp[i] == 3 && p.iup == -1))) continue;
-    const double dx = p.x[0] - cpx[3 * i], dy = p.x[1] - cpx[3 * i + 1], dz = p.x[2] - cpx[3 * i + 2];
-    const double d2i = dx * dx + dy * dy + dz * dz;
-    if (d2i < cp2) {
-      have = true;
-      idcp = i;
-      cp2 = d2i;
-      for (int j = 0; j < 3; j++) xcp[j] = cpx[3 * i + j];
-    }
-  }
+  Nearest n;
+  if (pre && pre->x[0] == p.x[0] && pre->x[1] == p.x[1] && pre->x[2] == p.x[2]) n = *pre;
+  else nearest_serial(p.x, p.iup, w, ncp, cpx, cptyp, n);
+  const bool have = n.have;
+  const int idcp = n.idcp;
+  const double cp2 = n.cp2;
+  double xcp[3] = {0, 0, 0};
+  if (have)
+    for (int j = 0; j < 3; j++) xcp[j] = n.isnuc ? w.xyz[3 * idcp + j] : cpx[3 * idcp + j];
   const double cprad = sqrt(cp2);
   if (have && cprad <= (rbeta ? rbeta[idcp] : kRBeta)) {
     p.incstep = true;

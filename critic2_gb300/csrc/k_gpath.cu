@@ -20,8 +20,11 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <vector>
+
+#include <math_constants.h>
 
 #include "c2g_internal.h"
 #include "gpath.h"
@@ -234,11 +237,12 @@ __device__ void ray_init(RayState &y, const Search &s, int att, int node) {
 }
 
 // Advances the ray until it needs the field at a point (true, x) or is done.
-__device__ bool ray_request(RayState &y, const Search &s, double x[3]) {
+// pre: the beta-sphere candidate for the path's position, or null.
+__device__ bool ray_request(RayState &y, const Search &s, double x[3], const Nearest *pre) {
   while (y.tracing) {
     Path &p = y.path;
     if (p.stage == 0) {
-      if (head(p, s.g, s.b.ncp, s.b.cpx, s.b.cptyp, y.own_rb ? s.rb : nullptr)) {
+      if (head(p, s.g, s.b.ncp, s.b.cpx, s.b.cptyp, y.own_rb ? s.rb : nullptr, pre)) {
         request_stage1(p);
         break;
       }
@@ -364,19 +368,65 @@ __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_ch
     }
   }
   __syncthreads();
-  if (tid == 0) {
-    for (int c = 0; c < 4; c++) q[c] = s_red[32 + c];
-    // the nucleus rule, at the wrapped point
-    for (int a = 0; a < w.natom; a++) {
+  if (wp == 0) {
+    // the nucleus rule at the wrapped point, the nuclei spread over warp 0
+    // (the square root only where the squared distance can pass)
+    bool near = false;
+    for (int a = lane; a < w.natom; a += 32) {
       const double4 A = w.atoms[a];
       const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
-      if (sqrt(dx * dx + dy * dy + dz * dz) <= 1e-5) {
-        q[1] = q[2] = q[3] = 0.0;
-        break;
-      }
+      const double dd = dx * dx + dy * dy + dz * dz;
+      if (dd <= 1.000001e-10 && sqrt(dd) <= 1e-5) near = true;
+    }
+    near = __any_sync(0xffffffffu, near);
+    if (lane == 0) {
+      for (int c = 0; c < 4; c++) q[c] = s_red[32 + c];
+      if (near) q[1] = q[2] = q[3] = 0.0;
     }
   }
   __syncthreads();
+}
+
+// Lexicographic minimum of (v, i) over the warp: the smallest value, and of
+// equal values the smallest index.
+__device__ void warp_min_first(double &v, int &i) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, off);
+    if (ov < v || (ov == v && oi < i)) v = ov, i = oi;
+  }
+}
+
+// nearest_serial by one warp (all 32 lanes, the same x): each lane scans
+// every 32nd nucleus and CP keeping its first minimum, and the lanes' minima
+// are merged by (value, index), so the candidate is the serial scan's.
+__device__ void nearest_warp(const double x[3], int iup, const PathGeom &w, int ncp, const double *cpx,
+                             const int *cptyp, Nearest &n) {
+  const int lane = threadIdx.x & 31;
+  double sph2 = 1e60;
+  int idnuc = 0;
+  for (int a = lane; a < w.natom; a += 32) {
+    const double dx = x[0] - w.xyz[3 * a], dy = x[1] - w.xyz[3 * a + 1], dz = x[2] - w.xyz[3 * a + 2];
+    const double d2a = dx * dx + dy * dy + dz * dz;
+    if (d2a < sph2) sph2 = d2a, idnuc = a;
+  }
+  warp_min_first(sph2, idnuc);
+  double c2 = CUDART_INF;
+  int ci = INT_MAX;
+  for (int i = lane; i < ncp; i += 32) {
+    if (!((cptyp[i] == -3 && iup == 1) || (cptyp[i] == 3 && iup == -1))) continue;
+    const double dx = x[0] - cpx[3 * i], dy = x[1] - cpx[3 * i + 1], dz = x[2] - cpx[3 * i + 2];
+    const double d2i = dx * dx + dy * dy + dz * dz;
+    if (d2i < c2) c2 = d2i, ci = i;
+  }
+  warp_min_first(c2, ci);
+  for (int j = 0; j < 3; j++) n.x[j] = x[j];
+  n.have = n.isnuc = false;
+  n.idcp = -1;
+  n.cp2 = 1e30;
+  if (iup == 1 && w.z[idnuc] != 1) n.have = n.isnuc = true, n.idcp = idnuc, n.cp2 = sph2;
+  if (c2 < n.cp2) n.have = true, n.isnuc = false, n.idcp = ci, n.cp2 = c2;
 }
 
 template <int MPT>
@@ -390,14 +440,28 @@ __global__ void __launch_bounds__(256) k_basin_rays(DevWfn w, PathGeom g, BasinD
   // the ray's state, used by thread 0 only (set by ray_init)
   __shared__ __align__(16) unsigned char s_ray[sizeof(RayState)];
   RayState &y = *reinterpret_cast<RayState *>(s_ray);
+  __shared__ long s_next;
   const Search s{g, b, b.rbeta_scratch + (size_t)blockIdx.x * (b.ncp > 0 ? b.ncp : 1)};
   const long nr = (long)b.natt * b.nray;
-  for (long ray = blockIdx.x; ray < nr; ray += gridDim.x) {
+  // rays are handed out in order by a counter: their costs differ severalfold
+  for (;;) {
+    if (threadIdx.x == 0) s_next = (long)atomicAdd(b.ray_next, 1ull);
+    __syncthreads();
+    const long ray = s_next;
+    if (ray >= nr) break;
     if (threadIdx.x == 0) ray_init(y, s, (int)(ray / b.nray), (int)(ray % b.nray));
     for (;;) {
+      // a path about to take a step: its beta-sphere candidate by warp 0
+      Nearest nc;
+      bool pre = false;
+      if (threadIdx.x < 32) {
+        __syncwarp();
+        pre = y.tracing && y.path.stage == 0;
+        if (pre) nearest_warp(y.path.x, y.path.iup, g, b.ncp, b.cpx, b.cptyp, nc);
+      }
       if (threadIdx.x == 0) {
         double x[3];
-        s_more = ray_request(y, s, x) ? 1 : 0;
+        s_more = ray_request(y, s, x, pre ? &nc : nullptr) ? 1 : 0;
         if (s_more) s_x[0] = x[0], s_x[1] = x[1], s_x[2] = x[2];
       }
       __syncthreads();
@@ -440,10 +504,18 @@ __global__ void __launch_bounds__(256) k_trace_paths(DevWfn w, PathGeom g, Paths
     long nev = 0;
     if (threadIdx.x == 0) start_path(p, d.x0 + 3 * i, d.iup[i], d.pathini + 3 * i);
     for (;;) {
+      // a path about to take a step: its beta-sphere candidate by warp 0
+      Nearest nc;
+      bool pre = false;
+      if (threadIdx.x < 32) {
+        __syncwarp();
+        pre = !p.done && p.stage == 0;
+        if (pre) nearest_warp(p.x, p.iup, g, d.ncp, d.cpx, d.cptyp, nc);
+      }
       if (threadIdx.x == 0) {
         bool need = p.stage == -1;
         while (!need && !p.done) {
-          if (p.stage == 0 && !head(p, g, d.ncp, d.cpx, d.cptyp, nullptr)) {
+          if (p.stage == 0 && !head(p, g, d.ncp, d.cpx, d.cptyp, nullptr, pre ? &nc : nullptr)) {
             p.done = true;
             break;
           }

@@ -25,6 +25,7 @@ struct BasinDev {
   double *rsurf;            // natt * nray
   int *ray_npath, *ray_nwarn, *ray_nrestart, *ray_err;  // err: 1 no bracket, 2 restarts, 3 evaluations
   long *ray_nevals;
+  unsigned long long *ray_next;  // the next ray to hand out (zero at launch)
 };
 
 // n single paths from x0 (3 * n) going iup (+1 up, -1 down), path length

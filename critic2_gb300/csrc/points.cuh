@@ -14,7 +14,11 @@ constexpr int kTilePoints = 32;
 __device__ __forceinline__ void wrap_cell(const DevWfn &w, double (&x)[3]) {
 #pragma unroll
   for (int j = 0; j < 3; j++) {
-    double f = (x[j] - w.cell_lo[j]) / w.cell_aa[j];
+    // within [-5e-5, 1 + 5e-5] cell lengths of the cell the quotient below
+    // is inside its bounds by far, and the point stays: no division
+    const double d = x[j] - w.cell_lo[j];
+    if (d >= -5e-5 * w.cell_aa[j] && d <= (1.0 + 5e-5) * w.cell_aa[j]) continue;
+    double f = d / w.cell_aa[j];
     if (f < -1e-4 || f > 1.0 + 1e-4) {
       f -= floor(f);
       x[j] = w.cell_lo[j] + f * w.cell_aa[j];
