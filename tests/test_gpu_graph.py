@@ -85,3 +85,24 @@ def test_graph_rejects_bad_types(gpu_lib):
         g.cp_graph(np.zeros((1, 3)), np.array([2], np.int32))
     out = g.cp_graph(np.zeros((0, 3)), np.zeros(0, np.int32))
     assert out["stats"]["npath"] == 0
+
+
+def test_graph_duplicate_cps_keep_first(gpu_lib, oracle_mod):
+    """The beta-sphere candidate is found by a warp (every lane scans every
+    32nd CP); equal distances must keep the first CP, as critic2's serial
+    scan does.  The CP list given twice over (more than 32 entries, so each
+    copy sits on another lane) yields the same terminators, all in the
+    first copy, and the same paths."""
+    from critic2_gb300.wfn import Wavefunction
+    mol = synth.make_molecule("nci12")
+    g, o = Wavefunction(mol), oracle_mod.Wfn(mol)
+    cp = o.autocritic()
+    x, t = cp["xyz"], cp["typ"]
+    n = len(t)
+    assert n > 32 and n % 32
+    one = g.cp_graph(x, t)
+    two = g.cp_graph(np.concatenate([x, x]), np.concatenate([t, t]))
+    for k in ("ipath", "brdist", "brpathlen", "ier", "nstep"):
+        assert np.array_equal(two[k][:n], one[k]), k
+        assert np.array_equal(two[k][n:], one[k]), k
+    assert np.all(two["ipath"] <= n)
