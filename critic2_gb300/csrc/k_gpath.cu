@@ -429,8 +429,10 @@ __device__ void nearest_warp(const double x[3], int iup, const PathGeom &w, int 
   if (c2 < n.cp2) n.have = true, n.isnuc = false, n.idcp = ci, n.cp2 = c2;
 }
 
+// Three blocks per SM (at most 85 registers a thread): the chain is
+// latency-bound on small molecules, FP64-bound on large ones.
 template <int MPT>
-__global__ void __launch_bounds__(256) k_basin_rays(DevWfn w, PathGeom g, BasinDev b) {
+__global__ void __launch_bounds__(256, 3) k_basin_rays(DevWfn w, PathGeom g, BasinDev b) {
   __shared__ double s_chi[256 * 4];
   __shared__ int s_k[256];
   __shared__ int s_wn[8];
@@ -491,7 +493,7 @@ __global__ void __launch_bounds__(256) k_basin_rays(DevWfn w, PathGeom g, BasinD
 // Single gradient paths (makegraph's), one block per path at a time: thread
 // 0 steps the path, the block evaluates the field it asks for.
 template <int MPT>
-__global__ void __launch_bounds__(256) k_trace_paths(DevWfn w, PathGeom g, PathsDev d) {
+__global__ void __launch_bounds__(256, 3) k_trace_paths(DevWfn w, PathGeom g, PathsDev d) {
   __shared__ double s_chi[256 * 4];
   __shared__ int s_k[256];
   __shared__ int s_wn[8];
