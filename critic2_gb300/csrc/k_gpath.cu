@@ -267,11 +267,25 @@ __device__ bool ray_request(RayState &y, const Search &s, double x[3], const Nea
   return true;
 }
 
+// Whether primitive pr, at squared distance dd from its atom, is within
+// its cutoff: !(sqrt(dd) > dran), decided without the square root except
+// within 1e-12 of the cutoff (the rounding of sqrt and of dran^2 is far
+// below that margin, so the answer is the same).
+__device__ __forceinline__ bool within_dran(double dd, double dran) {
+  const double r2 = dran * dran;
+  if (dd < r2 * (1.0 - 1e-12)) return true;
+  if (dd > r2 * (1.0 + 1e-12)) return false;
+  return !(sqrt(dd) > dran);
+}
+
 // The block's evaluation of rho and its gradient at x (wrapped into the
-// cell), into q[0..3] of thread 0.
+// cell), into q[0..3] of thread 0.  Per chunk of 256 primitives: the range
+// tests of all of them, the primitives in range compacted in primitive
+// order, their chi (the FP64 exponential and the Cartesian factors) by the
+// first threads, then the contraction.  s_d holds the compacted offsets.
 template <int MPT>
-__device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_chi, int *s_k, int *s_wn,
-                           double *s_red, double (&q)[4]) {
+__device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_chi, double *s_d, int *s_k,
+                           int *s_wn, double *s_red, double (&q)[4]) {
   const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
   double x[3] = {xin[0], xin[1], xin[2]};
   wrap_cell(w, x);
@@ -286,20 +300,14 @@ __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_ch
       for (int c = 0; c < 4; c++) acc[m][c] = 0.0;
     for (int k0 = 0; k0 < w.npri; k0 += 256) {
       const int ip = k0 + tid;
-      double chi[4];
+      double dx = 0.0, dy = 0.0, dz = 0.0, dd = 0.0;
       bool in = false;
       if (ip < w.npri) {
         const PrimF64 pr = w.prim[ip];
         const double4 A = w.atoms[pr.atom];
-        const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
-        const double dd = dx * dx + dy * dy + dz * dz;
-        if (dd <= A.w) {
-          const double dist = sqrt(dd);
-          if (!(dist > pr.dran)) {
-            in = true;
-            chi_eval<4>(dx, dy, dz, pr.e, pr.lpack, exp(-pr.e * (dist * dist)), chi);
-          }
-        }
+        dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+        dd = dx * dx + dy * dy + dz * dz;
+        in = dd <= A.w && within_dran(dd, pr.dran);
       }
       const unsigned bal = __ballot_sync(0xffffffffu, in);
       if (lane == 0) s_wn[wp] = __popc(bal);
@@ -312,9 +320,18 @@ __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_ch
       }
       if (in) {
         const int slot = base + __popc(bal & ((1u << lane) - 1u));
-#pragma unroll
-        for (int c = 0; c < 4; c++) s_chi[slot * 4 + c] = chi[c];
+        s_d[4 * slot] = dx, s_d[4 * slot + 1] = dy, s_d[4 * slot + 2] = dz, s_d[4 * slot + 3] = dd;
         s_k[slot] = ip;
+      }
+      __syncthreads();
+      if (tid < nact) {
+        const PrimF64 pr = w.prim[s_k[tid]];
+        const double dist = sqrt(s_d[4 * tid + 3]);
+        double chi[4];
+        chi_eval<4>(s_d[4 * tid], s_d[4 * tid + 1], s_d[4 * tid + 2], pr.e, pr.lpack, exp(-pr.e * (dist * dist)),
+                    chi);
+#pragma unroll
+        for (int c = 0; c < 4; c++) s_chi[tid * 4 + c] = chi[c];
       }
       __syncthreads();
       // threads without an MO skip the contraction (their sums stay zero)
@@ -434,6 +451,7 @@ __device__ void nearest_warp(const double x[3], int iup, const PathGeom &w, int 
 template <int MPT>
 __global__ void __launch_bounds__(256, 3) k_basin_rays(DevWfn w, PathGeom g, BasinDev b) {
   __shared__ double s_chi[256 * 4];
+  __shared__ double s_d[256 * 4];
   __shared__ int s_k[256];
   __shared__ int s_wn[8];
   __shared__ double s_red[8 * 4 + 4];
@@ -470,7 +488,7 @@ __global__ void __launch_bounds__(256, 3) k_basin_rays(DevWfn w, PathGeom g, Bas
       if (!s_more) break;
       const double xx[3] = {s_x[0], s_x[1], s_x[2]};
       double q[4];
-      eval_block<MPT>(w, xx, s_chi, s_k, s_wn, s_red, q);
+      eval_block<MPT>(w, xx, s_chi, s_d, s_k, s_wn, s_red, q);
       if (threadIdx.x == 0) {
         y.nevals++;
         double rec[4] = {q[0], q[1], q[2], q[3]};
@@ -495,6 +513,7 @@ __global__ void __launch_bounds__(256, 3) k_basin_rays(DevWfn w, PathGeom g, Bas
 template <int MPT>
 __global__ void __launch_bounds__(256, 3) k_trace_paths(DevWfn w, PathGeom g, PathsDev d) {
   __shared__ double s_chi[256 * 4];
+  __shared__ double s_d[256 * 4];
   __shared__ int s_k[256];
   __shared__ int s_wn[8];
   __shared__ double s_red[8 * 4 + 4];
@@ -532,7 +551,7 @@ __global__ void __launch_bounds__(256, 3) k_trace_paths(DevWfn w, PathGeom g, Pa
       if (!s_more) break;
       const double xx[3] = {s_x[0], s_x[1], s_x[2]};
       double q[4];
-      eval_block<MPT>(w, xx, s_chi, s_k, s_wn, s_red, q);
+      eval_block<MPT>(w, xx, s_chi, s_d, s_k, s_wn, s_red, q);
       if (threadIdx.x == 0) {
         nev++;
         if (p.stage == -1) take_start(p, q);
