@@ -58,6 +58,17 @@ __device__ __forceinline__ void chi_eval(double dx, double dy, double dz, double
   }
 }
 
+// Whether a primitive at squared distance dd from its atom is within its
+// cutoff: !(sqrt(dd) > dran), decided without the square root except
+// within 1e-12 of the cutoff (the rounding of sqrt and of dran^2 is far
+// below that margin, so the answer is the same).
+__device__ __forceinline__ bool within_dran(double dd, double dran) {
+  const double r2 = dran * dran;
+  if (dd < r2 * (1.0 - 1e-12)) return true;
+  if (dd > r2 * (1.0 + 1e-12)) return false;
+  return !(sqrt(dd) > dran);
+}
+
 // Adds EDF primitive i's c chi (value, gradient, Hessian) at x to core.
 __device__ __forceinline__ void edf_prim_add(const DevWfn &w, int i, const double (&x)[3], double (&core)[10]) {
   const PrimEDF pr = w.edf[i];

@@ -293,6 +293,7 @@ template <int MPT, class Src, class Sink>
 __global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, Src src, Sink sink) {
   constexpr int KC = 256;
   __shared__ double s_chi[KC * 10];
+  __shared__ double s_d[KC * 4];
   __shared__ int s_k[KC];
   __shared__ int s_wn[8];
   __shared__ double s_red[8 * kRecNci];
@@ -308,22 +309,19 @@ __global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, Src src, Sink si
 #pragma unroll
       for (int c = 0; c < 10; c++) acc[m][c] = 0.0;
     for (int k0 = 0; k0 < w.npri; k0 += KC) {
+      // the range tests of the chunk's primitives, those in range compacted
+      // in primitive order, then their chi on the first threads (a warp
+      // with one primitive in range would otherwise pay the whole FP64
+      // exponential)
       const int ip = k0 + tid;
-      double chi[10];
+      double dx = 0.0, dy = 0.0, dz = 0.0, dd = 0.0;
       bool in = false;
       if (ip < w.npri) {
         const PrimF64 pr = w.prim[ip];
         const double4 A = w.atoms[pr.atom];
-        const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
-        const double dd = dx * dx + dy * dy + dz * dz;
-        if (dd <= A.w) {
-          const double dist = sqrt(dd);
-          if (!(dist > pr.dran)) {
-            in = true;
-            const double ex = exp(-pr.e * (dist * dist));
-            chi_eval<10>(dx, dy, dz, pr.e, pr.lpack, ex, chi);
-          }
-        }
+        dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+        dd = dx * dx + dy * dy + dz * dz;
+        in = dd <= A.w && within_dran(dd, pr.dran);
       }
       const unsigned b = __ballot_sync(0xffffffffu, in);
       if (lane == 0) s_wn[wp] = __popc(b);
@@ -336,9 +334,18 @@ __global__ void __launch_bounds__(256) k_eval_fp64_pt(DevWfn w, Src src, Sink si
       }
       if (in) {
         const int slot = base + __popc(b & ((1u << lane) - 1u));
-#pragma unroll
-        for (int c = 0; c < 10; c++) s_chi[slot * 10 + c] = chi[c];
+        s_d[4 * slot] = dx, s_d[4 * slot + 1] = dy, s_d[4 * slot + 2] = dz, s_d[4 * slot + 3] = dd;
         s_k[slot] = ip;
+      }
+      __syncthreads();
+      if (tid < nact) {
+        const PrimF64 pr = w.prim[s_k[tid]];
+        const double dist = sqrt(s_d[4 * tid + 3]);
+        double chi[10];
+        chi_eval<10>(s_d[4 * tid], s_d[4 * tid + 1], s_d[4 * tid + 2], pr.e, pr.lpack, exp(-pr.e * (dist * dist)),
+                     chi);
+#pragma unroll
+        for (int c = 0; c < 10; c++) s_chi[tid * 10 + c] = chi[c];
       }
       __syncthreads();
       // threads without an MO skip the contraction (their sums stay zero)

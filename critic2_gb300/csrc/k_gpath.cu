@@ -267,17 +267,6 @@ __device__ bool ray_request(RayState &y, const Search &s, double x[3], const Nea
   return true;
 }
 
-// Whether primitive pr, at squared distance dd from its atom, is within
-// its cutoff: !(sqrt(dd) > dran), decided without the square root except
-// within 1e-12 of the cutoff (the rounding of sqrt and of dran^2 is far
-// below that margin, so the answer is the same).
-__device__ __forceinline__ bool within_dran(double dd, double dran) {
-  const double r2 = dran * dran;
-  if (dd < r2 * (1.0 - 1e-12)) return true;
-  if (dd > r2 * (1.0 + 1e-12)) return false;
-  return !(sqrt(dd) > dran);
-}
-
 // The block's evaluation of rho and its gradient at x (wrapped into the
 // cell), into q[0..3] of thread 0.  Per chunk of 256 primitives: the range
 // tests of all of them, the primitives in range compacted in primitive
