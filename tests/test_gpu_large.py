@@ -2,8 +2,8 @@
 3992 primitives, 400 MOs: four 128-MO tiles) and large500 (500 atoms,
 10003 primitives, 1000 MOs: eight MO tiles, per-tile atom tables in global
 memory).  Split precision against the GPU's FP64 form on i-planes of the
-real NCI grids (spec bars: |drho|/rho <= 1e-6, |ds| <= 1e-3, no sign
-flips), and the FP64 form against the oracle at 1e-10 on an f-shell patch
+real NCI grids (the split precision's bars: |drho|/rho <= 1e-6, |ds| <= 1e-3,
+no sign flips), and the FP64 form against the oracle at 1e-10 on an f-shell patch
 of prec200 and at scattered points of large500."""
 import numpy as np
 import pytest
@@ -62,7 +62,7 @@ def test_prec200_fp64_vs_oracle_f_shells(gpu_lib, oracle_mod):
 def test_large500_fp64_points_vs_oracle(gpu_lib, oracle_mod):
     """large500 (1000 MOs, eight MO tiles): rho2 at 200 scattered points in
     FP64 against the oracle at 1e-10, and TF32x3 against FP64 at the
-    spec density bar."""
+    split precision's density bar (1e-6)."""
     from critic2_gb300.wfn import Wavefunction
     mol = synth.make_molecule("large500")
     w, o = Wavefunction(mol), oracle_mod.Wfn(mol)

@@ -2,7 +2,7 @@
 
 The split modes are checked against the oracle (FP64) at random points and
 against the GPU's FP64 plain form on NCI grids.  Tolerances are the
-spec bars where they apply (|drho|/rho <= 1e-6 and |ds| <= 1e-3 for
+split precision's bars where they apply (|drho|/rho <= 1e-6 and |ds| <= 1e-3 for
 the 3-product TF32 split; the BF16 split carries 16 mantissa bits per
 operand pair and is held to 5e-5 relative)."""
 import numpy as np
@@ -12,7 +12,7 @@ from critic2_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
-# TF32x3: the spec bars (|drho|/rho <= 1e-6, |ds| <= 1e-3); BF16x3, a
+# TF32x3: the split precision's bars (|drho|/rho <= 1e-6, |ds| <= 1e-3); BF16x3, a
 # documented alternative that does not meet them, at its measured level
 TOL = {"tf32x3": dict(rho=1e-6, grad=2e-5, s=1e-3), "bf16x3": dict(rho=5e-5, grad=1e-3, s=1e-2)}
 
@@ -180,7 +180,7 @@ def test_g_and_h_shells_split():
     r64 = w.rho2(pts, 2, "fp64")
     # g and h primitives (l up to 5, powers of the offset formed by repeated
     # FP32 products) on a 0.15-bohr grid: measured 1.3e-6 for TF32x3, held to
-    # 2e-6; the spec configurations are s/p/d/f
+    # 2e-6; the bench workloads are s/p/d/f
     tol_rho = {"tf32x3": 2e-6, "bf16x3": TOL["bf16x3"]["rho"]}
     for prec in ("tf32x3", "bf16x3"):
         c, s, _ = w.nciplot(x0, xm, ns, prec)
