@@ -47,7 +47,7 @@ extern "C" {
 #define C2G_ERR_CUDA 2        /* a CUDA call failed, or no usable GPU */
 #define C2G_ERR_ALLOC 3       /* host or device allocation failed */
 #define C2G_ERR_IO 4          /* file could not be read or parsed */
-#define C2G_ERR_UNSUPPORTED 5 /* valid request this build does not support */
+#define C2G_ERR_UNSUPPORTED 5 /* valid request this library does not support */
 #define C2G_ERR_NUMERIC 6     /* the algorithm cannot complete on this input (critic2 stops there too) */
 
 /* arithmetic of the evaluation */

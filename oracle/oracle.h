@@ -4,8 +4,8 @@
  * TEST INFRASTRUCTURE ONLY.  This is a plain C (+OpenMP) restatement of
  * critic2's FP64 algorithm for the path (rho2 / calculate_mo_gto, field%grd,
  * the NCI grid loop, field%newton, field%addcp, autocritic pair seeding and
- * the Poincare-Hopf count).  It is the checker the GPU library's results are
- * compared against, and the timed CPU baseline ("port") in bench.py.  The
+ * the Poincare-Hopf count).  It is what the GPU library's results are
+ * compared against in the tests, and the timed CPU baseline ("port") in bench.py.  The
  * product library never links, loads or calls it.
  *
  * Parity status: the post-processing (3x3 eigen-solve, rank/signature, spin

@@ -1,7 +1,7 @@
 """ctypes wrapper of the C oracle (oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker, and by bench.py's CPU-baseline leg.  The product library
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+compare against, and by bench.py's CPU-baseline leg.  The product library
 (critic2_gb300) never imports this module.
 """
 from __future__ import annotations
