@@ -268,10 +268,13 @@ __device__ bool ray_request(RayState &y, const Search &s, double x[3], const Nea
 }
 
 // The block's evaluation of rho and its gradient at x (wrapped into the
-// cell), into q[0..3] of thread 0.  Per chunk of 256 primitives: the range
-// tests of all of them, the primitives in range compacted in primitive
-// order, their chi (the FP64 exponential and the Cartesian factors) by the
-// first threads, then the contraction.  s_d holds the compacted offsets.
+// cell), into q[0..3] of thread 0.  Per chunk of 256 primitives (atom-major,
+// so they span at most 256 atoms unless atoms without primitives lie
+// between): the offsets to the chunk's atoms once per atom, the range tests
+// of all primitives, those in range compacted in primitive order, their chi
+// (the FP64 exponential and the Cartesian factors) on the first threads,
+// then the contraction.  s_d holds the per-atom offsets and squared
+// distances (or, for a chunk spanning more atoms, the compacted primitives').
 template <int MPT>
 __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_chi, double *s_d, int *s_k,
                            int *s_wn, double *s_red, double (&q)[4]) {
@@ -289,14 +292,30 @@ __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_ch
       for (int c = 0; c < 4; c++) acc[m][c] = 0.0;
     for (int k0 = 0; k0 < w.npri; k0 += 256) {
       const int ip = k0 + tid;
+      const int a0 = w.prim[k0].atom, a1 = w.prim[min(k0 + 255, w.npri - 1)].atom;
+      const bool per_atom = a1 - a0 < 256;  // uniform over the block
+      if (per_atom && tid <= a1 - a0) {
+        const double4 A = w.atoms[a0 + tid];
+        const double dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+        s_d[4 * tid] = dx, s_d[4 * tid + 1] = dy, s_d[4 * tid + 2] = dz;
+        const double dd = dx * dx + dy * dy + dz * dz;
+        // beyond the atom's cutoff: marked by a negative squared distance
+        s_d[4 * tid + 3] = dd <= A.w ? dd : -1.0;
+      }
+      if (per_atom) __syncthreads();
       double dx = 0.0, dy = 0.0, dz = 0.0, dd = 0.0;
       bool in = false;
       if (ip < w.npri) {
         const PrimF64 pr = w.prim[ip];
-        const double4 A = w.atoms[pr.atom];
-        dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
-        dd = dx * dx + dy * dy + dz * dz;
-        in = dd <= A.w && within_dran(dd, pr.dran);
+        if (per_atom) {
+          dd = s_d[4 * (pr.atom - a0) + 3];
+          in = dd >= 0.0 && within_dran(dd, pr.dran);
+        } else {
+          const double4 A = w.atoms[pr.atom];
+          dx = x[0] - A.x, dy = x[1] - A.y, dz = x[2] - A.z;
+          dd = dx * dx + dy * dy + dz * dz;
+          in = dd <= A.w && within_dran(dd, pr.dran);
+        }
       }
       const unsigned bal = __ballot_sync(0xffffffffu, in);
       if (lane == 0) s_wn[wp] = __popc(bal);
@@ -307,18 +326,18 @@ __device__ void eval_block(const DevWfn &w, const double (&xin)[3], double *s_ch
         base += i < wp ? s_wn[i] : 0;
         nact += s_wn[i];
       }
-      if (in) {
-        const int slot = base + __popc(bal & ((1u << lane) - 1u));
-        s_d[4 * slot] = dx, s_d[4 * slot + 1] = dy, s_d[4 * slot + 2] = dz, s_d[4 * slot + 3] = dd;
-        s_k[slot] = ip;
+      const int slot = base + __popc(bal & ((1u << lane) - 1u));
+      if (in) s_k[slot] = ip;
+      if (!per_atom) {
+        if (in) s_d[4 * slot] = dx, s_d[4 * slot + 1] = dy, s_d[4 * slot + 2] = dz, s_d[4 * slot + 3] = dd;
       }
       __syncthreads();
       if (tid < nact) {
         const PrimF64 pr = w.prim[s_k[tid]];
-        const double dist = sqrt(s_d[4 * tid + 3]);
+        const double *o = s_d + 4 * (per_atom ? pr.atom - a0 : tid);
+        const double dist = sqrt(o[3]);
         double chi[4];
-        chi_eval<4>(s_d[4 * tid], s_d[4 * tid + 1], s_d[4 * tid + 2], pr.e, pr.lpack, exp(-pr.e * (dist * dist)),
-                    chi);
+        chi_eval<4>(o[0], o[1], o[2], pr.e, pr.lpack, exp(-pr.e * (dist * dist)), chi);
 #pragma unroll
         for (int c = 0; c < 4; c++) s_chi[tid * 4 + c] = chi[c];
       }
