@@ -49,10 +49,11 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 HEADLINE = "large500"
 EXTRA = ("prec200", "nci60")
 
-# DRAM bytes (read + write) per grid point of the split evaluator, from the
-# ncu captures summarised under profiles/ (traffic grows with the points; the
-# coefficient operands stay in L2).
-TRAFFIC_PER_POINT = {}
+# DRAM bytes (read + write) per grid point of the split evaluator's launch,
+# from the one-pass ncu capture of the whole 320^3 large500 launch
+# (profiles/k_tc_dram_large500_320cubed.md: 1.83 GB read + 1.76 GB written
+# over 32,768,000 points).
+TRAFFIC_PER_POINT = {("large500", "tf32x3"): (1.83e9 + 1.76e9) / 32768000}
 BASIN_NLEB = 26  # angular rule of the basin-integral part
 
 
