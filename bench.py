@@ -53,7 +53,7 @@ EXTRA = ("prec200", "nci60")
 # from the one-pass ncu capture of the whole 320^3 large500 launch
 # (profiles/k_tc_dram_large500_320cubed.md: 1.83 GB read + 1.76 GB written
 # over 32,768,000 points).
-TRAFFIC_PER_POINT = {("large500", "tf32x3"): (1.83e9 + 1.76e9) / 32768000}
+TRAFFIC_PER_POINT = {("large500", "tf32x3", 320): (1.83e9 + 1.76e9) / 32768000}
 BASIN_NLEB = 26  # angular rule of the basin-integral part
 
 
@@ -418,7 +418,7 @@ def roofline_of(res, mol, npri, prec, pk, pk_kind, wl):
     issued = active * nmt * 2.0 * 128 * ISSUED_COLUMNS_PER_STAGE * kps
     peak = pk["bf16_tflops"] if prec == "bf16x3" else pk["bf16_tflops"] / 2.0
     ach = issued / t / 1e12
-    trf = TRAFFIC_PER_POINT.get((wl.name, prec))
+    trf = TRAFFIC_PER_POINT.get((wl.name, prec, wl.grid))
     return {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
             "traffic": None if trf is None else trf * npts,
             "note": (f"achieved = MMA work issued by the split kernel (M 128 x N {ISSUED_COLUMNS_PER_STAGE} x "
