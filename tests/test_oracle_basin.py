@@ -197,3 +197,32 @@ def test_sphere_integrals_one_center(oracle_mod):
         assert abs(pop - ref) <= 1e-10 * abs(ref)
         assert abs(lap - 4 * np.pi * R * R * (-2 * b * R) * rho_r) <= 1e-9 * abs(4 * np.pi * R * R * 2 * b * R * rho_r)
     assert np.allclose(r["radii"][0], 0.1 * np.exp(np.arange(6) * np.log(30.0) / 5), rtol=1e-14)
+
+
+def test_sphere_quadrature_golden(oracle_mod):
+    """critic2's SPHEREINTEGRALS regression output (a crystal field, so only
+    its field-independent columns, tests/golden/make_sphere_golden.py): the
+    logarithmic radii r0 exp(h (n - 1)) and each sphere's volume, the
+    angular rule's weight sum times r^3 / 3, for GAULEG 2 2 and LEBEDEV 6.
+    The oracle's radii and this file's GAULEG and Lebedev weights (the ones
+    the GPU tests hold the library's rays and integrals to) reproduce them
+    to the printed digits."""
+    import json
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "sphere_quadrature.json")))
+    mol = diatomic()
+    w = oracle_mod.Wfn(mol)
+    cpx, cpt = mol.atom_xyz.copy(), np.array([-3, -3], np.int32)
+    for b in gold["blocks"]:
+        if b["angular"] == "gauleg":
+            u, wa, ring, ringw = gauleg_rays(b["ntheta"], b["nphi"])
+            wsum = float(np.sum(ringw[ring] * wa))
+            kw = dict(ring=ring, ringw=ringw)
+        else:
+            u, wu = lebedev_rays(oracle_mod, b["nleb"])
+            wa, wsum, kw = wu, float(np.sum(wu)), {}
+        r = w.sphere_integrals(cpx, cpt, u, wa, cpid=1, nr=b["nr"], r0=b["r0"], rend=b["rend"], **kw)
+        radii = r["radii"][0]
+        assert abs(np.log(b["rend"] / b["r0"]) / (b["nr"] - 1) - b["h"]) <= 1e-6 * b["h"]
+        for row, rr in zip(b["rows"], radii):
+            assert abs(rr - row["r"]) <= 1e-6 * row["r"]
+            assert abs(wsum * rr ** 3 / 3.0 - row["volume"]) <= 1e-8 * row["volume"]
