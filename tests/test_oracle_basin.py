@@ -226,3 +226,16 @@ def test_sphere_quadrature_golden(oracle_mod):
         for row, rr in zip(b["rows"], radii):
             assert abs(rr - row["r"]) <= 1e-6 * row["r"]
             assert abs(wsum * rr ** 3 / 3.0 - row["volume"]) <= 1e-8 * row["volume"]
+
+
+@pytest.mark.parametrize("n", [6, 14, 26, 110, 170, 194, 302, 590, 770])
+def test_library_lebedev_matches_fixture(oracle_mod, n):
+    """The library's tables (lebedev_tables.h) and the independently
+    generated rules of tests/golden/lebedev_rules.json (the oracle's) hold
+    the same points and weights."""
+    lib = library_rule(n)
+    ref = oracle_mod.lebedev_rule(n)
+    d = np.linalg.norm(lib[:, None, :3] - ref[None, :, :3], axis=2)
+    j = d.argmin(1)
+    assert d.min(1).max() < 1e-13 and len(set(j)) == n
+    assert np.allclose(lib[:, 3], ref[j, 3], rtol=1e-12, atol=1e-15)
