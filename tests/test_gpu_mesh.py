@@ -61,6 +61,8 @@ def test_molcalc_gaussian_known_answer(gpu_lib):
     r = g.molcalc(("rho",), "franchini", "good")
     assert r["npoints"] == 219252
     assert abs(r["rho"] / exact - 1) < 3e-7
+    # critic2's benzene meshes, small level (tests/011_mesh/ref/001_meshtype.cro)
+    assert g.mesh_size("franchini", "small") == 55440 and g.mesh_size("becke", "small") == 55440
 
 
 @pytest.mark.parametrize("mesh", ["franchini", "becke"])

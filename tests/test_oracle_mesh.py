@@ -1,7 +1,8 @@
 """Molecular meshes in the oracle (genmesh_becke / genmesh_franchini,
 src/meshmod@proc.f90:79-627) and the Lebedev rules they use.  Pins: the
-mesh size critic2 reports for benzene (tests/004_load/ref/002_load-wfx.cro:
-"Mesh size 219252", Franchini, good), the exactness of the angular rules,
+mesh sizes critic2 reports for benzene (tests/004_load/ref/002_load-wfx.cro:
+"Mesh size 219252", Franchini, good; tests/011_mesh/ref/001_meshtype.cro:
+55440, Franchini and Becke, small), the exactness of the angular rules,
 the library's compressed Lebedev table against the fixture, and the
 convergence of the integral of a normalised Gaussian density."""
 import itertools
@@ -70,9 +71,13 @@ def test_library_table_matches_fixture(oracle_mod):
 
 def test_mesh_size_of_benzene(oracle_mod):
     # critic2: "Mesh size 219252", Franchini, good, for benzene (6 C, 6 H)
+    # (tests/004_load/ref/002_load-wfx.cro), and "Mesh size 55440" for
+    # Franchini and Becke, small (tests/011_mesh/ref/001_meshtype.cro)
     w = oracle_mod.Wfn(benzene_like())
     xyz, wt = w.mesh("franchini", "good")
     assert len(wt) == 219252
+    for mesh in ("franchini", "becke"):
+        assert len(w.mesh(mesh, "small")[1]) == 55440
     assert oracle_mod.lib().o_z2nr(1, 3) == 52 and oracle_mod.lib().o_z2nr(6, 3) == 69
 
 
