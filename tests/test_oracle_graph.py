@@ -116,3 +116,35 @@ def test_graph_is_deterministic(oracle_mod, graph12):
     g2 = w.makegraph(cp["xyz"], cp["typ"], nthreads=1)
     for k in g:
         assert np.array_equal(g[k], g2[k])
+
+
+def test_graph_duplicate_cps_keep_first(oracle_mod, graph12):
+    """critic2's scan for the nearest beta sphere keeps the first CP of equal
+    distance: with the CP list given twice over, every terminator is in the
+    first copy and every path is the same (the library's warp-parallel scan
+    is held to the same rule by the GPU test of the same name)."""
+    mol, cp, g = graph12
+    w = oracle_mod.Wfn(mol)
+    n = len(cp["typ"])
+    two = w.makegraph(np.concatenate([cp["xyz"], cp["xyz"]]), np.concatenate([cp["typ"], cp["typ"]]))
+    for k in ("ipath", "brdist", "brpathlen", "ier", "nstep"):
+        assert np.array_equal(two[k][:n], g[k]) and np.array_equal(two[k][n:], g[k]), k
+    assert np.all(two["ipath"] <= n)
+
+
+def test_range_test_without_square_root():
+    """The device evaluators decide !(sqrt(dd) > dran) without the square
+    root except within 1e-12 of dran^2.  In IEEE double arithmetic (numpy)
+    that gives the same answer as the square root on squared distances a few
+    ulps either side of the cutoff, and far from it, over a range of
+    cutoffs."""
+    rng = np.random.default_rng(7)
+    dran = np.exp(rng.uniform(np.log(0.3), np.log(40.0), 4000))
+    r2 = dran * dran
+    near = np.concatenate([r2 * (1 + k * 2.0 ** -52) for k in range(-8, 9)])
+    far = np.concatenate([r2 * f for f in (0.5, 1 - 2e-12, 1 - 1e-12, 1 + 1e-12, 1 + 2e-12, 2.0)])
+    dd = np.concatenate([near, far])
+    dr = np.tile(dran, len(dd) // len(dran))
+    rr = dr * dr
+    fast = np.where(dd < rr * (1 - 1e-12), True, np.where(dd > rr * (1 + 1e-12), False, ~(np.sqrt(dd) > dr)))
+    assert np.array_equal(fast, ~(np.sqrt(dd) > dr))
